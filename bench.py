@@ -1,0 +1,284 @@
+"""Benchmark: CI sigma throughput on the 16-orbital synthetic FCI workload.
+
+Workload (one step = one sigma = H C over all determinants for 4 roots):
+FCI of 16 spatial orbitals with 8 alpha + 8 beta electrons, 12,870 strings per
+spin, 165,636,900 determinants, 4 roots, seeded synthetic integrals
+(polyquant_gb300.synthetic.fci_integrals, seed 0).  C (5.3 GB in FP64) is larger
+than L2, so no flush is needed between steps.
+
+Printed JSON line (rank 0):
+  value   : sigma dets/s = n_dets * roots / t_sigma, FP64 kernel, inputs resident in HBM
+  e2e     : the same metric through pq_ci_sigma_host with pinned host buffers (H2D + sigma + D2H)
+  mixed   : the FP32 sigma kernel (the bulk sigma of the mixed-precision Davidson)
+  roofline: compulsory bytes B = n_dets*roots*(8+8) + n_dets*8 per FP64 sigma over the kernel time,
+            against the measured HBM copy bandwidth
+  cpu_baseline: the CPU oracle (C restatement of the reference sigma, OpenMP) on a row sample
+
+--impl reference runs only the CPU baseline (reference algorithm restated) on the
+same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+N_ORB, N_A, N_B, ROOTS, SEED = 16, 8, 8, 4, 0
+METRIC = "sigma dets/s"
+UNIT = "dets/s"
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_problem():
+    from polyquant_gb300 import synthetic
+
+    h, eri = synthetic.fci_integrals(N_ORB, seed=SEED)
+    return h, eri
+
+
+def cpu_baseline(C_host=None, budget_s=15.0, threads=None):
+    """Time the oracle's gather sigma (the reference's element formulas, OpenMP) on a row sample."""
+    import oracle as O
+
+    h, eri = make_problem()
+    prob = O.CIProblem([N_ORB], [N_A], [N_B], [[h, h]], {(0, 0, 0, 0): eri}, [[8, 8, 16]])
+    t0 = time.time()
+    ds = O.Detset(prob, check_addressing=False)
+    setup = time.time() - t0
+    n = ds.n_dets
+    if C_host is None:
+        C_host = np.zeros((n, ROOTS), order="F")
+        C_host[:] = np.random.default_rng(1).standard_normal((n, ROOTS))
+    threads = threads or os.cpu_count()
+    rng = np.random.default_rng(2)
+    rows_done, elapsed, batch = 0, 0.0, 256
+    while elapsed < budget_s:
+        rows = rng.choice(n, size=batch, replace=False)
+        t0 = time.time()
+        ds.sigma_rows(C_host, rows, nthreads=threads)
+        dt = time.time() - t0
+        elapsed += dt
+        rows_done += batch
+        if dt < budget_s / 8:
+            batch *= 2
+    return {"value": rows_done * ROOTS / elapsed, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{rows_done} random rows of the 165,636,900-determinant sigma (4 roots), "
+                      f"{elapsed:.1f} s of CPU time on {threads} threads; setup {setup:.1f} s excluded"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    cb = cpu_baseline(budget_s=args.cpu_budget)
+    per_step = cb["value"]
+    line = {"metric": METRIC, "value": per_step, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 165636900 * ROOTS / per_step * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "FCI 16 orbitals 8a+8b, 165,636,900 determinants, 4 roots, seed 0",
+                       "precision": "fp64"},
+            "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": per_step, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from polyquant_gb300._lib import PQ_FP32, PQ_FP64, check, load
+    from polyquant_gb300.detset import POLYQUANT_DETSET
+
+    L = load()
+    h, eri = make_problem()
+    t0 = time.time()
+    ds = POLYQUANT_DETSET([N_ORB], [N_A], [N_B], [[h, h]], {(0, 0, 0, 0): eri}, [[8, 8, 16]])
+    torch.cuda.synchronize()
+    setup_s = time.time() - t0
+    n = ds.N_dets
+    stream = torch.cuda.current_stream().cuda_stream
+    # interleaved FP64 / FP32 buffers (det-major, 4 roots)
+    gen = torch.Generator(device="cuda").manual_seed(1 + rank)
+    X64 = torch.randn(n, ROOTS, device="cuda", dtype=torch.float64, generator=gen)
+    X64 /= X64.norm(dim=0, keepdim=True)
+    Y64 = torch.empty_like(X64)
+    X32 = X64.float()
+    Y32 = torch.empty_like(X32)
+
+    def sigma(prec):
+        X, Y = (X64, Y64) if prec == PQ_FP64 else (X32, Y32)
+        check(L.pq_ci_sigma_interleaved(ds._h, ctypes.c_void_p(X.data_ptr()), ctypes.c_void_p(Y.data_ptr()), ROOTS,
+                                        prec, ctypes.c_double(0.0)), "sigma")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(prec, steps, warmup):
+        for _ in range(warmup):
+            sigma(prec)
+        barrier()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(steps):
+            sigma(prec)
+        ev1.record()
+        barrier()
+        ms = ev0.elapsed_time(ev1) / steps
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = t.item()
+        return ms
+
+    with ClockSampler(local) as clk:
+        ms64 = timed(PQ_FP64, args.steps, args.warmup)
+    ms32 = timed(PQ_FP32, max(args.steps, 3), args.warmup)
+    units = n * ROOTS * world
+    value = units / (ms64 * 1e-3)
+    hbm, peak_kind = peaks()
+    bytes_alg = n * ROOTS * 16 + n * 8
+    achieved = bytes_alg / (ms64 * 1e-3) / 1e9
+
+    e2e = None
+    if not args.no_e2e:
+        # public API with host buffers: pinned column-major C (n x 4) in, sigma out
+        Ch = torch.empty((ROOTS, n), dtype=torch.float64, pin_memory=True)
+        Ch.copy_(X64.t())
+        Sh = torch.empty((ROOTS, n), dtype=torch.float64, pin_memory=True)
+        for _ in range(max(1, args.warmup // 2)):
+            check(L.pq_ci_sigma_host(ds._h, ctypes.c_void_p(Ch.data_ptr()), n, ROOTS, ctypes.c_void_p(Sh.data_ptr()), n,
+                                     PQ_FP64), "sigma_host")
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            check(L.pq_ci_sigma_host(ds._h, ctypes.c_void_p(Ch.data_ptr()), n, ROOTS, ctypes.c_void_p(Sh.data_ptr()), n,
+                                     PQ_FP64), "sigma_host")
+        barrier()
+        dt = (time.perf_counter() - t0) / args.steps
+        # check the host result against the device result
+        err = (Sh.t().cuda() - Y64).abs().max().item() / Y64.abs().max().item()
+        e2e = {"value": units / dt, "unit": UNIT, "h2d_bytes_per_step": n * ROOTS * 8, "d2h_bytes_per_step": n * ROOTS * 8,
+               "ms_per_step": dt * 1e3, "rel_diff_vs_device": err}
+
+    cb = None
+    if rank == 0 and not args.no_cpu:
+        cb = cpu_baseline(budget_s=args.cpu_budget)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms64, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "FCI 16 orbitals 8a+8b, 165,636,900 determinants, 4 roots, seed 0",
+                           "precision": "fp64", "l2": "inputs (5.3 GB) larger than L2; no flush",
+                           "parallelism": "replicas" if world > 1 else "single GPU",
+                           "setup_seconds": setup_s},
+                "e2e": e2e,
+                "mixed": {"value": units / (ms32 * 1e-3), "unit": UNIT, "ms_per_step": ms32, "dtype": "f32"},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                             "frac": achieved / hbm, "traffic": None, "peak_source": peak_kind,
+                             "algorithmic_bytes_per_launch": bytes_alg},
+                "gpu_launches": args.steps,
+                "clocks": clk.summary(),
+                "cpu_baseline": cb}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,144 @@
+/*
+ * pq_ci.h -- C ABI of the GB300 CI sigma library (libpq_gb300.so).
+ *
+ * Drop-in replacement for the determinant-space operator that polyquant's
+ * Davidson driver calls.  Reference interfaces replaced (paths inside the
+ * polyquant project):
+ *
+ *   POLYQUANT_DETSET<uint64_t>::rows()/cols()        src/ci/determinant_set.hpp:127-134
+ *   POLYQUANT_DETSET<uint64_t>::operator()(i, i)     src/ci/determinant_set.hpp:139
+ *   POLYQUANT_DETSET<uint64_t>::operator*(X)         src/ci/determinant_set.hpp:170, src/ci/detset/direct.cpp:5-18
+ *   POLYQUANT_DETSET<uint64_t>::create_sigma         src/ci/detset/direct.cpp:21-33
+ *   POLYQUANT_DETSET<uint64_t>::precompute_diagonal_Slater_Condon  src/ci/detset/slater_condon.cpp:102-153
+ *   POLYQUANT_EPCI::setup_determinants               src/ci/epci.cpp:334-388
+ *   Spectra::DavidsonSymEigsSolver<DETSET>::compute  (driver call site src/ci/epci.cpp:589-608)
+ *
+ * Conventions: every function returns a pq_status; nothing calls exit().  The
+ * message of the last failure on the calling thread is pq_last_error().  Host
+ * buffers belong to the caller, device buffers created by the library belong
+ * to the handle.  Calls on one handle are ordered on its CUDA stream; a handle
+ * is used by one host thread at a time.  Sizes are int64.
+ */
+#ifndef PQ_CI_H
+#define PQ_CI_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t pq_status;
+enum {
+  PQ_OK = 0,
+  PQ_ERR_ARG = 1,         /* invalid argument or unsupported problem */
+  PQ_ERR_CUDA = 2,        /* a CUDA runtime or library call failed */
+  PQ_ERR_OOM = 3,         /* device allocation failed */
+  PQ_NOT_CONVERGED = 4,   /* Davidson hit its iteration limit; results are the last iterate */
+  PQ_TIMEOUT = 5,         /* a bounded device wait gave up */
+  PQ_ERR_STATE = 6        /* call out of order (e.g. no GPU, handle destroyed) */
+};
+
+enum { PQ_FP64 = 0, PQ_FP32 = 1 };
+
+/* Message of the last failing call on this host thread ("" if none). */
+const char *pq_last_error(void);
+/* Library version string. */
+const char *pq_version(void);
+
+/*
+ * One CI problem, in the reference's conventions.
+ *  n_orb        active orbitals per species (POLYQUANT_DETSET::max_orb)
+ *  n_alpha/beta active particles per spin (frozen core already removed)
+ *  restricted   1: one spin block of integrals (the reference's `1 % size` rule)
+ *  charge       species charge; cross-species terms carry charge[0]*charge[1]
+ *  ex_level     {alpha max, beta max, total max} per species
+ *               (POLYQUANT_EPCI::excitation_level, ci_keywords "excitation_level")
+ *  max_collective  limit on the summed excitation of all species
+ *  h1[s][spin]  n_orb x n_orb MO one-body integrals (column-major, host)
+ *  eri[a][sa][b][sb]  (npair_a x npair_b) MO ERIs, column-major, element
+ *               [idx2(i,j) + idx2(k,l)*npair_a] = (ij|kl), b >= a, host
+ *               (POLYQUANT_INTEGRAL::mo_two_body_ints, integral.cpp:479-516)
+ * Pointers of the spin index 1 may be NULL for restricted species.
+ */
+typedef struct {
+  int32_t n_species;
+  int32_t n_orb[2];
+  int32_t n_alpha[2];
+  int32_t n_beta[2];
+  int32_t restricted[2];
+  double charge[2];
+  int32_t ex_level[2][3];
+  int32_t max_collective;
+  const double *h1[2][2];
+  const double *eri[2][2][2][2];
+} pq_ci_desc;
+
+typedef struct pq_ci_handle pq_ci_handle;
+
+/* Build strings, excitation tables, determinant addressing and the diagonal
+ * on the device (replaces setup_determinants + precompute_diagonal).
+ * stream: a cudaStream_t, or NULL for the default stream. */
+pq_status pq_ci_create(const pq_ci_desc *desc, void *stream, pq_ci_handle **out);
+pq_status pq_ci_destroy(pq_ci_handle *h);
+
+/* rows() == cols() == number of determinants. */
+pq_status pq_ci_num_dets(const pq_ci_handle *h, int64_t *n_dets);
+/* Strings of one species/spin in the reference layout: n_words per string,
+ * word 0 holds the highest orbitals (determinant_creation.cpp:13, 62-68).
+ * words == NULL queries n_strings and n_words only. */
+pq_status pq_ci_strings(const pq_ci_handle *h, int32_t species, int32_t spin, uint64_t *words, int64_t *n_strings,
+                        int32_t *n_words);
+/* Unfolded string indices of every determinant, n_dets x (2*n_species), host
+ * buffer (det_idx_unfold, determinant_creation.cpp:378-388). */
+pq_status pq_ci_det_unfold(const pq_ci_handle *h, int32_t *out);
+/* Diagonal H_II (operator()(i,i)); out is a DEVICE buffer of n_dets doubles. */
+pq_status pq_ci_diag(pq_ci_handle *h, double *out_device);
+
+/* sigma = H C for nvec vectors (operator*).  C and S are DEVICE buffers,
+ * column-major n_dets x nvec with leading dimensions ldc, lds (the Eigen layout
+ * the reference passes).  precision: PQ_FP64 or PQ_FP32 (FP32 tables and
+ * arithmetic, inputs/outputs still FP64). */
+pq_status pq_ci_sigma(pq_ci_handle *h, const double *C, int64_t ldc, int32_t nvec, double *S, int64_t lds,
+                      int32_t precision);
+/* Same with HOST buffers: copies in, computes, copies out (blocking). */
+pq_status pq_ci_sigma_host(pq_ci_handle *h, const double *C, int64_t ldc, int32_t nvec, double *S, int64_t lds,
+                           int32_t precision);
+
+/* Native-layout sigma on DEVICE buffers interleaved by determinant:
+ * X[det * nvec + v].  T = double (precision PQ_FP64) or float (PQ_FP32).
+ * diag_shift is subtracted from H_II (sigma = (H - shift*1) X). */
+pq_status pq_ci_sigma_interleaved(pq_ci_handle *h, const void *X, void *Y, int32_t nvec, int32_t precision,
+                                  double diag_shift);
+
+/* Block Davidson on the GPU (replaces Spectra::DavidsonSymEigsSolver with the
+ * reference's parameters: initial = num_subspace_vec, max = max(2*initial,
+ * 10*num_states), epci.cpp:589-590). */
+typedef struct {
+  int32_t num_states;
+  int32_t num_subspace_vec;
+  int32_t max_subspace;      /* <= 0: max(2*num_subspace_vec, 10*num_states) */
+  int32_t iteration_max;     /* ci_keywords "iteration_max" (default 500) */
+  double convergence_E;      /* residual-norm tolerance (ci_keywords "convergence_E") */
+  int32_t precision;         /* PQ_FP64, or PQ_FP32 = FP32 sigma with FP64 refinement */
+  double energy_shift;       /* added to eigenvalues (E_nuc + frozen-core energy) */
+  int32_t verbose;           /* 1: per-iteration table on stdout */
+} pq_davidson_params;
+
+typedef struct {
+  int32_t iterations;
+  int32_t sigma_calls_fp64;
+  int32_t sigma_calls_fp32;
+  int32_t converged;
+  double max_residual;
+  double seconds;
+} pq_davidson_report;
+
+/* energies: host, num_states doubles (shift included).  vecs: DEVICE buffer
+ * n_dets x num_states column-major, or NULL. */
+pq_status pq_ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *energies, double *vecs,
+                         pq_davidson_report *report);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,377 @@
+// Block Davidson eigensolver on the GPU for the lowest roots of H.
+//
+// Replaces the reference's use of Spectra::DavidsonSymEigsSolver
+// (src/ci/epci.cpp:589-608): initial subspace = unit vectors at the smallest
+// diagonal elements, diagonal preconditioner (theta - H_II)^-1, convergence
+// when every residual norm is below convergence_E, subspace limits
+// initial = num_subspace_vec and max = max(2*initial, 10*num_states).
+// Spectra itself is not part of the reference tree; this solver is pinned by
+// the converged energies only.
+//
+// All subspace algebra (Gram-Schmidt, projections, Ritz vectors, residual
+// norms, preconditioner denominators) is FP64 on the device through cuBLAS;
+// the Rayleigh matrix eigenproblem (at most a few hundred rows) is solved on
+// the host in FP64.  With precision = PQ_FP32 the sigma vectors of new search
+// directions come from the FP32 kernel applied to (H - s) with s the current
+// lowest Ritz value, and every restart recomputes the Ritz vectors' sigma in
+// FP64 ("residual refinement"), so reported energies and residual norms are
+// always exact FP64 Rayleigh quotients and residuals.
+#include <cublas_v2.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <numeric>
+#include <vector>
+
+#include "pq_internal.h"
+
+namespace pq {
+
+#define PQ_CUBLAS_TRY(call)                                                          \
+  do {                                                                               \
+    cublasStatus_t cs_ = (call);                                                     \
+    if (cs_ != CUBLAS_STATUS_SUCCESS) {                                              \
+      set_error("%s failed: cublas status %d (%s:%d)", #call, (int)cs_, __FILE__, __LINE__); \
+      return PQ_ERR_CUDA;                                                            \
+    }                                                                                \
+  } while (0)
+
+// Cyclic Jacobi eigensolver for a small symmetric matrix (column-major n x n).
+// Eigenvalues ascending in w, eigenvectors in the columns of Z.
+static void jacobi_eigh(int n, std::vector<double> A, std::vector<double> &w, std::vector<double> &Z) {
+  Z.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; i++) Z[i + (size_t)i * n] = 1.0;
+  auto a = [&](int i, int j) -> double & { return A[i + (size_t)j * n]; };
+  for (int sweep = 0; sweep < 100; sweep++) {
+    double off = 0.0, tot = 0.0;
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++) {
+        tot += a(i, j) * a(i, j);
+        if (i != j) off += a(i, j) * a(i, j);
+      }
+    if (off <= 1e-30 * std::max(tot, 1e-300)) break;
+    for (int p = 0; p < n - 1; p++)
+      for (int q = p + 1; q < n; q++) {
+        double apq = a(p, q);
+        if (std::fabs(apq) < 1e-300) continue;
+        double theta = (a(q, q) - a(p, p)) / (2.0 * apq);
+        double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; k++) {
+          double akp = a(k, p), akq = a(k, q);
+          a(k, p) = c * akp - s * akq;
+          a(k, q) = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; k++) {
+          double apk = a(p, k), aqk = a(q, k);
+          a(p, k) = c * apk - s * aqk;
+          a(q, k) = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; k++) {
+          double zkp = Z[k + (size_t)p * n], zkq = Z[k + (size_t)q * n];
+          Z[k + (size_t)p * n] = c * zkp - s * zkq;
+          Z[k + (size_t)q * n] = s * zkp + c * zkq;
+        }
+      }
+  }
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::sort(order.begin(), order.end(), [&](int x, int y) { return a(x, x) < a(y, y); });
+  std::vector<double> Zs((size_t)n * n);
+  w.resize(n);
+  for (int j = 0; j < n; j++) {
+    w[j] = a(order[j], order[j]);
+    for (int i = 0; i < n; i++) Zs[i + (size_t)j * n] = Z[i + (size_t)order[j] * n];
+  }
+  Z.swap(Zs);
+}
+
+__global__ void unit_vectors_kernel(double *V, int64_t n, const int64_t *idx, int m) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (; i < n * m; i += stride) {
+    int64_t c = i / n, r = i - c * n;
+    V[i] = (idx[c] == r) ? 1.0 : 0.0;
+  }
+}
+
+// T[:, j] = R[:, j] / (theta_j - D)   (diagonal preconditioner)
+__global__ void precondition_kernel(const double *R, const double *D, const double *theta, int64_t n, int k,
+                                    double *T) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (; i < n * k; i += stride) {
+    int64_t c = i / n, r = i - c * n;
+    double den = theta[c] - D[r];
+    if (fabs(den) < 1e-8) den = den < 0 ? -1e-8 : 1e-8;
+    T[i] = R[i] / den;
+  }
+}
+
+// W[:, j] = Y_il[:, j] + s * V[:, j] from the interleaved FP32 sigma of (H - s)
+__global__ void unshift_kernel(const float *Y, int nvp, int nv, const double *V, int64_t ldv, double s, int64_t n,
+                               double *W, int64_t ldw) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (; i < n; i += stride)
+    for (int v = 0; v < nv; v++) W[i + v * ldw] = (double)Y[i * nvp + v] + s * V[i + v * ldv];
+}
+
+struct Davidson {
+  pq_ci_handle *h;
+  cublasHandle_t cb = nullptr;
+  int64_t n = 0;
+  DevBuf V, W, X, R, T, tmp, dth, didx, coef;
+  ~Davidson() {
+    if (cb) cublasDestroy(cb);
+  }
+  unsigned grid() const { return (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16); }
+
+  // sigma for nv columns of src (ld n) into dst (ld n); FP32 path applies shift s
+  pq_status sigma(const double *src, double *dst, int nv, int precision, double s, pq_davidson_report *rep) {
+    if (precision == PQ_FP64) {
+      for (int v0 = 0; v0 < nv; v0 += 4) {
+        int c = std::min(4, nv - v0), nvp = c == 1 ? 1 : (c == 2 ? 2 : 4);
+        PQ_TRY(h->x_il.ensure(sizeof(double) * nvp * (size_t)(n + 1)));
+        PQ_TRY(h->y_il.ensure(sizeof(double) * nvp * (size_t)(n + 1)));
+        PQ_TRY(ci_to_il(h, src, n, v0, c, nvp, PQ_FP64, h->x_il.ptr));
+        PQ_TRY(ci_sigma_il(h, h->x_il.ptr, h->y_il.ptr, nvp, PQ_FP64, 0.0));
+        PQ_TRY(ci_from_il(h, h->y_il.ptr, v0, c, nvp, PQ_FP64, dst, n));
+      }
+      rep->sigma_calls_fp64++;
+    } else {
+      for (int v0 = 0; v0 < nv; v0 += 4) {
+        int c = std::min(4, nv - v0), nvp = c == 1 ? 1 : (c == 2 ? 2 : 4);
+        PQ_TRY(h->x_il.ensure(sizeof(float) * nvp * (size_t)(n + 1)));
+        PQ_TRY(h->y_il.ensure(sizeof(float) * nvp * (size_t)(n + 1)));
+        PQ_TRY(ci_to_il(h, src, n, v0, c, nvp, PQ_FP32, h->x_il.ptr));
+        PQ_TRY(ci_sigma_il(h, h->x_il.ptr, h->y_il.ptr, nvp, PQ_FP32, s));
+        unshift_kernel<<<grid(), 256, 0, h->stream>>>((const float *)h->y_il.ptr, nvp, c, src + (size_t)v0 * n, n, s, n,
+                                                       dst + (size_t)v0 * n, n);
+        PQ_CUDA_TRY(cudaGetLastError());
+      }
+      rep->sigma_calls_fp32++;
+    }
+    return PQ_OK;
+  }
+
+  // G = V[:, 0:m]^T W[:, 0:m] on the host (symmetrised)
+  pq_status rayleigh(int m, std::vector<double> &G) {
+    PQ_TRY(tmp.ensure(sizeof(double) * (size_t)m * m));
+    const double one = 1.0, zero = 0.0;
+    PQ_CUBLAS_TRY(cublasDgemm(cb, CUBLAS_OP_T, CUBLAS_OP_N, m, m, (int)n, &one, V.as<double>(), (int)n, W.as<double>(),
+                              (int)n, &zero, tmp.as<double>(), m));
+    G.resize((size_t)m * m);
+    PQ_CUDA_TRY(cudaMemcpyAsync(G.data(), tmp.ptr, sizeof(double) * m * m, cudaMemcpyDeviceToHost, h->stream));
+    PQ_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    for (int i = 0; i < m; i++)
+      for (int j = i + 1; j < m; j++) {
+        double s = 0.5 * (G[i + (size_t)j * m] + G[j + (size_t)i * m]);
+        G[i + (size_t)j * m] = G[j + (size_t)i * m] = s;
+      }
+    return PQ_OK;
+  }
+
+  // Orthonormalise columns T[:, 0:k] against V[:, 0:m] and each other (two
+  // classical Gram-Schmidt passes); accepted columns are appended to V.
+  pq_status orthonormalize_append(int m, int k, int *added) {
+    const double one = 1.0, mone = -1.0, zero = 0.0;
+    PQ_TRY(coef.ensure(sizeof(double) * (size_t)(m + k) * 2));
+    int mm = m;
+    for (int j = 0; j < k; j++) {
+      double *t = T.as<double>() + (size_t)j * n;
+      double nrm0 = 0.0;
+      PQ_CUBLAS_TRY(cublasDnrm2(cb, (int)n, t, 1, &nrm0));
+      if (!(nrm0 > 0.0) || !std::isfinite(nrm0)) continue;
+      for (int pass = 0; pass < 2; pass++) {
+        PQ_CUBLAS_TRY(cublasDgemv(cb, CUBLAS_OP_T, (int)n, mm, &one, V.as<double>(), (int)n, t, 1, &zero,
+                                  coef.as<double>(), 1));
+        PQ_CUBLAS_TRY(cublasDgemv(cb, CUBLAS_OP_N, (int)n, mm, &mone, V.as<double>(), (int)n, coef.as<double>(), 1,
+                                  &one, t, 1));
+      }
+      double nrm = 0.0;
+      PQ_CUBLAS_TRY(cublasDnrm2(cb, (int)n, t, 1, &nrm));
+      if (!(nrm > 1e-8 * nrm0) || nrm < 1e-300) continue;
+      double inv = 1.0 / nrm;
+      PQ_CUBLAS_TRY(cublasDscal(cb, (int)n, &inv, t, 1));
+      PQ_CUDA_TRY(cudaMemcpyAsync(V.as<double>() + (size_t)mm * n, t, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                  h->stream));
+      mm++;
+    }
+    *added = mm - m;
+    return PQ_OK;
+  }
+};
+
+pq_status ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *energies, double *vecs,
+                      pq_davidson_report *rep_out) {
+  auto t_start = std::chrono::steady_clock::now();
+  pq_davidson_report rep{};
+  Davidson D;
+  D.h = h;
+  D.n = h->n_dets;
+  const int64_t n = D.n;
+  int k = p->num_states;
+  if (k < 1 || n < 1) {
+    set_error("davidson: num_states=%d, n_dets=%lld", k, (long long)n);
+    return PQ_ERR_ARG;
+  }
+  if (p->precision != PQ_FP64 && p->precision != PQ_FP32) {
+    set_error("davidson: precision must be PQ_FP64 or PQ_FP32");
+    return PQ_ERR_ARG;
+  }
+  if (n > 0x7fffffffLL) {
+    set_error("davidson: n_dets beyond the 32-bit cuBLAS dimension limit");
+    return PQ_ERR_ARG;
+  }
+  int m0 = std::max(p->num_subspace_vec, k);
+  int mmax = p->max_subspace > 0 ? p->max_subspace : std::max(2 * p->num_subspace_vec, 10 * k);
+  mmax = std::max(mmax, m0 + k);
+  if ((int64_t)m0 > n) m0 = (int)n;
+  if ((int64_t)mmax > n) mmax = (int)n;
+  if (k > m0) {
+    set_error("davidson: num_states %d exceeds the space dimension %lld", k, (long long)n);
+    return PQ_ERR_ARG;
+  }
+  const int iter_max = p->iteration_max > 0 ? p->iteration_max : 500;
+  const double tol = p->convergence_E > 0 ? p->convergence_E : 1e-6;
+  cudaStream_t st = h->stream;
+  if (cublasCreate(&D.cb) != CUBLAS_STATUS_SUCCESS) {
+    set_error("cublasCreate failed");
+    return PQ_ERR_CUDA;
+  }
+  PQ_CUBLAS_TRY(cublasSetStream(D.cb, st));
+  PQ_TRY(D.V.alloc(sizeof(double) * (size_t)n * mmax));
+  PQ_TRY(D.W.alloc(sizeof(double) * (size_t)n * mmax));
+  PQ_TRY(D.X.alloc(sizeof(double) * (size_t)n * k));
+  PQ_TRY(D.R.alloc(sizeof(double) * (size_t)n * k));
+  PQ_TRY(D.T.alloc(sizeof(double) * (size_t)n * std::max(k, m0)));
+  PQ_TRY(D.dth.alloc(sizeof(double) * std::max(k, 8)));
+
+  // initial subspace: unit vectors at the m0 smallest diagonal elements
+  std::vector<double> diag(n);
+  PQ_CUDA_TRY(cudaMemcpyAsync(diag.data(), h->d_diag.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  PQ_CUDA_TRY(cudaStreamSynchronize(st));
+  std::vector<int64_t> idx(n);
+  std::iota(idx.begin(), idx.end(), 0);
+  auto cmp = [&](int64_t a, int64_t b) { return diag[a] < diag[b] || (diag[a] == diag[b] && a < b); };
+  std::partial_sort(idx.begin(), idx.begin() + m0, idx.end(), cmp);
+  idx.resize(m0);
+  double shift = diag[idx[0]];
+  PQ_TRY(upload(D.didx, idx, st));
+  unit_vectors_kernel<<<D.grid(), 256, 0, st>>>(D.V.as<double>(), n, D.didx.as<int64_t>(), m0);
+  PQ_CUDA_TRY(cudaGetLastError());
+  // unit vectors are exact in FP32: their sigma is computed in FP64 to start
+  PQ_TRY(D.sigma(D.V.as<double>(), D.W.as<double>(), m0, PQ_FP64, 0.0, &rep));
+  int m = m0;
+  bool exact = true;  // every column of W is an FP64 sigma
+  std::vector<double> G, w, Z;
+  std::vector<double> theta(k), rnorm(k);
+  const double one = 1.0, mone = -1.0, zero = 0.0;
+  int it = 0;
+  bool force_refine = false;
+  pq_status result = PQ_NOT_CONVERGED;
+  for (it = 1; it <= iter_max; it++) {
+    PQ_TRY(D.rayleigh(m, G));
+    jacobi_eigh(m, G, w, Z);
+    for (int i = 0; i < k; i++) theta[i] = w[i];
+    PQ_TRY(D.tmp.ensure(sizeof(double) * (size_t)m * k));
+    std::vector<double> Yk(Z.begin(), Z.begin() + (size_t)m * k);
+    PQ_CUDA_TRY(cudaMemcpyAsync(D.tmp.ptr, Yk.data(), sizeof(double) * m * k, cudaMemcpyHostToDevice, st));
+    // X = V Y, R = W Y - X theta
+    PQ_CUBLAS_TRY(cublasDgemm(D.cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, k, m, &one, D.V.as<double>(), (int)n,
+                              D.tmp.as<double>(), m, &zero, D.X.as<double>(), (int)n));
+    PQ_CUBLAS_TRY(cublasDgemm(D.cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, k, m, &one, D.W.as<double>(), (int)n,
+                              D.tmp.as<double>(), m, &zero, D.R.as<double>(), (int)n));
+    double maxr = 0.0;
+    for (int i = 0; i < k; i++) {
+      double mt = -theta[i];
+      PQ_CUBLAS_TRY(cublasDaxpy(D.cb, (int)n, &mt, D.X.as<double>() + (size_t)i * n, 1, D.R.as<double>() + (size_t)i * n, 1));
+      PQ_CUBLAS_TRY(cublasDnrm2(D.cb, (int)n, D.R.as<double>() + (size_t)i * n, 1, &rnorm[i]));
+      maxr = std::max(maxr, rnorm[i]);
+    }
+    if (p->verbose) {
+      printf("davidson it %3d  m %3d  %s", it, m, exact ? "fp64" : "mixd");
+      for (int i = 0; i < k; i++) printf("  E%d % .12f r %.2e", i, theta[i] + p->energy_shift, rnorm[i]);
+      printf("\n");
+    }
+    rep.max_residual = maxr;
+    bool small = maxr < tol;
+    if (small && exact) {
+      result = PQ_OK;
+      break;
+    }
+    // restart when the subspace cannot take another block, or refine the
+    // mixed-precision subspace once its residuals look converged
+    bool refine = !exact && (small || force_refine);
+    bool need_restart = (m + k > mmax) || refine;
+    force_refine = false;
+    if (need_restart) {
+      int r = refine ? k : std::min(m0, m);
+      r = std::max(r, k);
+      // V[:, 0:r] = V Z[:, 0:r]; W likewise (via the temporary T)
+      PQ_TRY(D.tmp.ensure(sizeof(double) * (size_t)m * r));
+      std::vector<double> Zr(Z.begin(), Z.begin() + (size_t)m * r);
+      PQ_CUDA_TRY(cudaMemcpyAsync(D.tmp.ptr, Zr.data(), sizeof(double) * m * r, cudaMemcpyHostToDevice, st));
+      PQ_TRY(D.T.ensure(sizeof(double) * (size_t)n * r));
+      PQ_CUBLAS_TRY(cublasDgemm(D.cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, r, m, &one, D.V.as<double>(), (int)n,
+                                D.tmp.as<double>(), m, &zero, D.T.as<double>(), (int)n));
+      PQ_CUDA_TRY(cudaMemcpyAsync(D.V.ptr, D.T.ptr, sizeof(double) * n * r, cudaMemcpyDeviceToDevice, st));
+      if (p->precision == PQ_FP32) {
+        // FP64 refinement: exact sigma of the restart vectors
+        PQ_TRY(D.sigma(D.V.as<double>(), D.W.as<double>(), r, PQ_FP64, 0.0, &rep));
+        exact = true;
+      } else {
+        PQ_CUBLAS_TRY(cublasDgemm(D.cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, r, m, &one, D.W.as<double>(), (int)n,
+                                  D.tmp.as<double>(), m, &zero, D.T.as<double>(), (int)n));
+        PQ_CUDA_TRY(cudaMemcpyAsync(D.W.ptr, D.T.ptr, sizeof(double) * n * r, cudaMemcpyDeviceToDevice, st));
+      }
+      m = r;
+      continue;
+    }
+    // corrections for unconverged roots
+    int nt = 0;
+    std::vector<double> th_u;
+    for (int i = 0; i < k; i++) {
+      if (rnorm[i] < tol) continue;
+      PQ_CUDA_TRY(cudaMemcpyAsync(D.T.as<double>() + (size_t)nt * n, D.R.as<double>() + (size_t)i * n,
+                                  sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+      th_u.push_back(theta[i]);
+      nt++;
+    }
+    PQ_CUDA_TRY(cudaMemcpyAsync(D.dth.ptr, th_u.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, st));
+    precondition_kernel<<<D.grid(), 256, 0, st>>>(D.T.as<double>(), h->d_diag.as<double>(), D.dth.as<double>(), n, nt,
+                                                  D.T.as<double>());
+    PQ_CUDA_TRY(cudaGetLastError());
+    int added = 0;
+    PQ_TRY(D.orthonormalize_append(m, nt, &added));
+    if (added == 0) {
+      // no new direction: the subspace is invariant to working precision
+      if (exact) {
+        result = PQ_OK;
+        break;
+      }
+      force_refine = true;
+      continue;
+    }
+    shift = theta[0];
+    PQ_TRY(D.sigma(D.V.as<double>() + (size_t)m * n, D.W.as<double>() + (size_t)m * n, added, p->precision, shift,
+                   &rep));
+    if (p->precision == PQ_FP32) exact = false;
+    m += added;
+  }
+  rep.iterations = std::min(it, iter_max);
+  rep.converged = result == PQ_OK;
+  for (int i = 0; i < k; i++) energies[i] = theta[i] + p->energy_shift;
+  if (vecs) PQ_CUDA_TRY(cudaMemcpyAsync(vecs, D.X.ptr, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, st));
+  PQ_CUDA_TRY(cudaStreamSynchronize(st));
+  rep.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  if (rep_out) *rep_out = rep;
+  if (result != PQ_OK) set_error("davidson: not converged after %d iterations (max residual %.3e)", iter_max, rep.max_residual);
+  (void)mone;
+  return result;
+}
+
+}  // namespace pq

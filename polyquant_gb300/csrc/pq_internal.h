@@ -1,0 +1,109 @@
+// Internal declarations shared by the CUDA translation units of libpq_gb300.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "pq_ci.h"
+#include "pq_ints.h"
+
+namespace pq {
+
+// Thread-local error message behind pq_last_error().
+void set_error(const char *fmt, ...);
+void clear_error();
+
+#define PQ_CUDA_TRY(call)                                                                                  \
+  do {                                                                                                     \
+    cudaError_t e_ = (call);                                                                               \
+    if (e_ != cudaSuccess) {                                                                               \
+      pq::set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);           \
+      return e_ == cudaErrorMemoryAllocation ? PQ_ERR_OOM : PQ_ERR_CUDA;                                   \
+    }                                                                                                      \
+  } while (0)
+
+#define PQ_TRY(expr)                   \
+  do {                                 \
+    pq_status s_ = (expr);             \
+    if (s_ != PQ_OK) return s_;        \
+  } while (0)
+
+// Device buffer owned by a handle.
+struct DevBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  ~DevBuf() { release(); }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+  pq_status alloc(size_t n);
+  // grow-only allocation used for scratch; contents are not preserved
+  pq_status ensure(size_t n) { return n <= bytes ? PQ_OK : alloc(n); }
+  template <typename T> T *as() const { return static_cast<T *>(ptr); }
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+};
+
+template <typename T> pq_status upload(DevBuf &b, const std::vector<T> &v, cudaStream_t s) {
+  PQ_TRY(b.alloc(v.size() * sizeof(T) + 16));
+  if (!v.empty()) PQ_CUDA_TRY(cudaMemcpyAsync(b.ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  return PQ_OK;
+}
+
+// Excitation tables of one spin list of one species (CSR over strings).
+// Single entries: J (string index), info = (pair << 1) | (phase < 0), and the
+// same-spin part of the element F = h_hp + sum_{k in occ(I)} ((hp|kk) - (hk|kp)).
+// Double entries: J and the full same-spin element value.
+struct SpinTablesDev {
+  int64_t n_str = 0;
+  int64_t n1 = 0, n2 = 0;  // total entries
+  int32_t max1 = 0, max2 = 0;
+  DevBuf str;              // uint64 occupation masks, bit o = orbital o
+  DevBuf s1_off, s1_J, s1_info, s1_F64, s1_F32;
+  DevBuf s2_off, s2_J, s2_D64, s2_D32;
+  DevBuf e_same64;         // per-string same-spin energy (diagonal part)
+};
+
+}  // namespace pq
+
+struct pq_ci_handle {
+  pq_ci_desc desc{};
+  cudaStream_t stream = nullptr;
+  int n_species = 1;
+  int n_orb[2] = {0, 0};
+  int npair[2] = {0, 0};
+  int n_words = 1;
+  int n_blocks[2] = {1, 1};  // spin blocks of integrals per species
+  // host strings (occupation masks, reference order) and their levels
+  std::vector<uint64_t> str[2][2];
+  std::vector<int32_t> lvl[2][2];
+  // determinant addressing over species-0 alpha strings (single species)
+  int64_t n_dets = 0;
+  bool full = false;  // every (alpha, beta) pair present
+  std::vector<int64_t> rowoff;
+  std::vector<int32_t> rowlen;
+  pq::DevBuf d_rowoff, d_rowlen;
+  pq::SpinTablesDev tab[2][2];
+  // cross-spin ERI block (pair_alpha | pair_beta), row-major, per precision
+  pq::DevBuf d_eab64, d_eab32;
+  pq::DevBuf d_diag;
+  // scratch for layout conversion
+  pq::DevBuf x_il, y_il;
+};
+
+namespace pq {
+// ci_setup.cu
+pq_status ci_build(pq_ci_handle *h);
+// ci_sigma.cu
+pq_status ci_sigma_il(pq_ci_handle *h, const void *X, void *Y, int nvec, int precision, double shift);
+pq_status ci_to_il(pq_ci_handle *h, const double *C, int64_t ldc, int v0, int nv, int nvp, int precision, void *X);
+pq_status ci_from_il(pq_ci_handle *h, const void *Y, int v0, int nv, int nvp, int precision, double *S, int64_t lds);
+// ci_davidson.cu
+pq_status ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *energies, double *vecs,
+                      pq_davidson_report *rep);
+}  // namespace pq

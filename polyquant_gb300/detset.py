@@ -1,0 +1,195 @@
+"""Host-side mirror of polyquant's determinant-set operator on the GB300 library.
+
+``POLYQUANT_DETSET`` keeps the reference's operator interface
+(src/ci/determinant_set.hpp:120-170): ``rows()``, ``cols()``, ``op(i, i)``
+(the diagonal, slater_condon.cpp:5-7), ``op * X`` / ``op @ X`` (sigma,
+direct.cpp:5-18) and ``create_sigma(sigma, C)`` (direct.cpp:21-33).  Every
+operation calls the C ABI of libpq_gb300.so; there is no CPU path.
+
+Inputs follow the reference conventions: MO one-body integrals per species and
+spin, MO ERI blocks (npair_a x npair_b, [idx2(i,j), idx2(k,l)]), excitation
+levels {alpha, beta, total} per species and the collective limit.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Dict, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _lib
+from ._lib import PQ_FP32, PQ_FP64, check
+
+INT_MAX = 2 ** 31 - 1
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+class POLYQUANT_DETSET:
+    """Determinant space + Hamiltonian operator built on the GPU.
+
+    Parameters mirror ``pq_ci_desc``: ``h1[s][spin]`` (n x n) and
+    ``eri[(a, sa, b, sb)]`` (npair_a x npair_b) as numpy arrays; restricted
+    species need only spin index 0.
+    """
+
+    Scalar = float
+
+    def __init__(self, n_orb: Sequence[int], n_alpha: Sequence[int], n_beta: Sequence[int], h1, eri: Dict,
+                 excitation_level: Sequence[Sequence[int]], restricted: Sequence[int] = None,
+                 charge: Sequence[float] = None, max_collective_excitation_level: int = INT_MAX, stream=None):
+        L = _lib.load()
+        ns = len(n_orb)
+        restricted = list(restricted) if restricted is not None else [1] * ns
+        charge = list(charge) if charge is not None else [-1.0] * ns
+        d = _lib.PQDesc()
+        d.n_species = ns
+        self._keep = []
+        for s in range(ns):
+            d.n_orb[s] = int(n_orb[s])
+            d.n_alpha[s] = int(n_alpha[s])
+            d.n_beta[s] = int(n_beta[s])
+            d.restricted[s] = int(restricted[s])
+            d.charge[s] = float(charge[s])
+            for t in range(3):
+                d.ex_level[s][t] = int(excitation_level[s][t])
+            nb = 1 if restricted[s] else 2
+            for sp in range(2):
+                m = np.asfortranarray(np.asarray(h1[s][sp % nb] if len(h1[s]) > sp % nb else h1[s][0],
+                                                 dtype=np.float64))
+                self._keep.append(m)
+                d.h1[s][sp] = m.ctypes.data
+        d.max_collective = int(max_collective_excitation_level)
+        for a in range(ns):
+            for sa in range(2):
+                for b in range(a, ns):
+                    for sb in range(2):
+                        key = (a, sa % (1 if restricted[a] else 2), b, sb % (1 if restricted[b] else 2))
+                        m = eri.get(key)
+                        if m is None and a == b and (a, key[3], a, key[1]) in eri:
+                            m = np.asarray(eri[(a, key[3], a, key[1])]).T
+                        if m is None:
+                            continue
+                        m = np.asfortranarray(np.asarray(m, dtype=np.float64))
+                        self._keep.append(m)
+                        d.eri[a][sa][b][sb] = m.ctypes.data
+        self._desc = d
+        self._stream = stream
+        h = ctypes.c_void_p()
+        check(L.pq_ci_create(ctypes.byref(d), ctypes.c_void_p(stream or 0), ctypes.byref(h)), "pq_ci_create")
+        self._h = h
+        self._keep = []  # integrals were copied to the device
+        n = ctypes.c_int64()
+        check(L.pq_ci_num_dets(self._h, ctypes.byref(n)))
+        self.N_dets = n.value
+        self.n_species = ns
+        self._diag = None
+
+    # ---- lifetime ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().pq_ci_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- Spectra operator concept ------------------------------------------
+    def rows(self) -> int:
+        return self.N_dets
+
+    def cols(self) -> int:
+        return self.N_dets
+
+    def diagonal(self):
+        """Device tensor of H_II (torch.float64, cuda)."""
+        torch = _torch()
+        if self._diag is None:
+            out = torch.empty(self.N_dets, dtype=torch.float64, device="cuda")
+            check(_lib.load().pq_ci_diag(self._h, ctypes.c_void_p(out.data_ptr())), "pq_ci_diag")
+            self._diag = out
+        return self._diag
+
+    def __call__(self, i: int, j: int) -> float:
+        if i != j:
+            raise NotImplementedError("only diagonal elements are exposed (the Davidson preconditioner needs H_II)")
+        return float(self.diagonal()[i].item())
+
+    def sigma(self, C, precision: int = PQ_FP64):
+        """sigma = H C.  C: torch CUDA tensor (n_dets,) or (n_dets, k) float64, or a numpy array."""
+        if isinstance(C, np.ndarray):
+            return self._sigma_host(C, precision)
+        torch = _torch()
+        squeeze = C.dim() == 1
+        X = C.reshape(self.N_dets, -1)
+        # column-major n x k == row-major k x n
+        Xc = X.t().contiguous().to(torch.float64)
+        S = torch.empty_like(Xc)
+        k = Xc.shape[0]
+        check(_lib.load().pq_ci_sigma(self._h, ctypes.c_void_p(Xc.data_ptr()), self.N_dets, k,
+                                      ctypes.c_void_p(S.data_ptr()), self.N_dets, precision), "pq_ci_sigma")
+        out = S.t()
+        return out.reshape(-1) if squeeze else out
+
+    def _sigma_host(self, C: np.ndarray, precision: int):
+        squeeze = C.ndim == 1
+        X = np.asfortranarray(np.asarray(C, dtype=np.float64).reshape(self.N_dets, -1))
+        S = np.zeros_like(X, order="F")
+        check(_lib.load().pq_ci_sigma_host(self._h, X.ctypes.data, self.N_dets, X.shape[1], S.ctypes.data,
+                                           self.N_dets, precision), "pq_ci_sigma_host")
+        return S.reshape(-1) if squeeze else S
+
+    def __mul__(self, X):
+        return self.sigma(X)
+
+    __matmul__ = __mul__
+
+    def create_sigma(self, sigma, C):
+        """In-place form of the reference's create_sigma(sigma, C) (sigma is overwritten)."""
+        sigma[...] = self.sigma(C)
+        return sigma
+
+    # ---- strings / determinants ----------------------------------------------
+    def strings(self, species: int, spin: int) -> np.ndarray:
+        L = _lib.load()
+        n = ctypes.c_int64()
+        nw = ctypes.c_int32()
+        check(L.pq_ci_strings(self._h, species, spin, None, ctypes.byref(n), ctypes.byref(nw)))
+        out = np.zeros((n.value, nw.value), dtype=np.uint64)
+        check(L.pq_ci_strings(self._h, species, spin, out.ctypes.data, ctypes.byref(n), ctypes.byref(nw)))
+        return out
+
+    def det_unfold(self) -> np.ndarray:
+        out = np.zeros((self.N_dets, 2 * self.n_species), dtype=np.int32)
+        check(_lib.load().pq_ci_det_unfold(self._h, out.ctypes.data))
+        return out
+
+    # ---- eigen-solver ----------------------------------------------------------
+    def davidson(self, num_states: int = 1, num_subspace_vec: int = 5, iteration_max: int = 500,
+                 convergence_E: float = 1e-6, precision: int = PQ_FP64, energy_shift: float = 0.0,
+                 max_subspace: int = 0, return_vectors: bool = False, verbose: bool = False):
+        torch = _torch()
+        p = _lib.PQDavidsonParams(num_states, num_subspace_vec, max_subspace, iteration_max, convergence_E, precision,
+                                  energy_shift, 1 if verbose else 0)
+        e = np.zeros(num_states, dtype=np.float64)
+        rep = _lib.PQDavidsonReport()
+        vecs = None
+        vptr = None
+        if return_vectors:
+            vecs = torch.empty((num_states, self.N_dets), dtype=torch.float64, device="cuda")
+            vptr = ctypes.c_void_p(vecs.data_ptr())
+        st = _lib.load().pq_ci_davidson(self._h, ctypes.byref(p), e.ctypes.data, vptr, ctypes.byref(rep))
+        check(st, "pq_ci_davidson")
+        info = dict(iterations=rep.iterations, converged=bool(rep.converged), max_residual=rep.max_residual,
+                    sigma_calls_fp64=rep.sigma_calls_fp64, sigma_calls_fp32=rep.sigma_calls_fp32,
+                    seconds=rep.seconds)
+        if return_vectors:
+            return e, vecs.t(), info
+        return e, info
