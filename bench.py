@@ -109,12 +109,19 @@ def make_problem():
     return h, eri
 
 
+def workload_name():
+    from math import comb
+
+    nd = comb(N_ORB, N_A) * comb(N_ORB, N_B)
+    return f"FCI {N_ORB} orbitals {N_A}a+{N_B}b, {nd:,} determinants, {ROOTS} roots, seed {SEED}"
+
+
 def cpu_baseline(C_host=None, budget_s=15.0, threads=None):
     """Time the oracle's gather sigma (the reference's element formulas, OpenMP) on a row sample."""
     import oracle as O
 
     h, eri = make_problem()
-    prob = O.CIProblem([N_ORB], [N_A], [N_B], [[h, h]], {(0, 0, 0, 0): eri}, [[8, 8, 16]])
+    prob = O.CIProblem([N_ORB], [N_A], [N_B], [[h, h]], {(0, 0, 0, 0): eri}, [[N_A, N_B, N_A + N_B]])
     t0 = time.time()
     ds = O.Detset(prob, check_addressing=False)
     setup = time.time() - t0
@@ -134,8 +141,8 @@ def cpu_baseline(C_host=None, budget_s=15.0, threads=None):
         rows_done += batch
         if dt < budget_s / 8:
             batch *= 2
-    return {"value": rows_done * ROOTS / elapsed, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{rows_done} random rows of the 165,636,900-determinant sigma (4 roots), "
+    return {"value": rows_done * ROOTS / elapsed, "unit": UNIT, "cores": threads, "kind": "port", "n_dets": n,
+            "sample": f"{rows_done} random rows of the {n:,}-determinant sigma ({ROOTS} roots), "
                       f"{elapsed:.1f} s of CPU time on {threads} threads; setup {setup:.1f} s excluded"}
 
 
@@ -145,10 +152,9 @@ def run_reference(args, rank, world):
     cb = cpu_baseline(budget_s=args.cpu_budget)
     per_step = cb["value"]
     line = {"metric": METRIC, "value": per_step, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 165636900 * ROOTS / per_step * 1e3, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": cb["n_dets"] * ROOTS / per_step * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "FCI 16 orbitals 8a+8b, 165,636,900 determinants, 4 roots, seed 0",
-                       "precision": "fp64"},
+            "config": {"workload": workload_name(), "precision": "fp64"},
             "impl": "reference", "cpu_baseline": cb,
             "e2e": {"value": per_step, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -163,7 +169,10 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--norb", type=int, default=N_ORB, help="smaller FCI case for profiling only")
+    ap.add_argument("--nel", type=int, default=N_A, help="electrons per spin of the profiling case")
     args = ap.parse_args()
+    globals().update(N_ORB=args.norb, N_A=args.nel, N_B=args.nel)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -185,7 +194,8 @@ def main():
     L = load()
     h, eri = make_problem()
     t0 = time.time()
-    ds = POLYQUANT_DETSET([N_ORB], [N_A], [N_B], [[h, h]], {(0, 0, 0, 0): eri}, [[8, 8, 16]])
+    ds = POLYQUANT_DETSET([N_ORB], [N_A], [N_B], [[h, h]], {(0, 0, 0, 0): eri},
+                          [[N_A, N_B, N_A + N_B]])
     torch.cuda.synchronize()
     setup_s = time.time() - t0
     n = ds.N_dets
@@ -263,8 +273,7 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms64, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": "FCI 16 orbitals 8a+8b, 165,636,900 determinants, 4 roots, seed 0",
-                           "precision": "fp64", "l2": "inputs (5.3 GB) larger than L2; no flush",
+                "config": {"workload": workload_name(), "precision": "fp64", "l2": "inputs (5.3 GB) larger than L2; no flush",
                            "parallelism": "replicas" if world > 1 else "single GPU",
                            "setup_seconds": setup_s},
                 "e2e": e2e,

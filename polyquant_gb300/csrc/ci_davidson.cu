@@ -272,6 +272,10 @@ pq_status ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *ener
   const double one = 1.0, mone = -1.0, zero = 0.0;
   int it = 0;
   bool force_refine = false;
+  bool phase32 = p->precision == PQ_FP32;
+  bool just_refined = false;
+  double last_refined = 1e300;
+  const double switch_tol = std::max(tol, 1e-5);
   pq_status result = PQ_NOT_CONVERGED;
   for (it = 1; it <= iter_max; it++) {
     PQ_TRY(D.rayleigh(m, G));
@@ -298,14 +302,19 @@ pq_status ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *ener
       printf("\n");
     }
     rep.max_residual = maxr;
-    bool small = maxr < tol;
-    if (small && exact) {
+    if (maxr < tol && exact) {
       result = PQ_OK;
       break;
     }
-    // restart when the subspace cannot take another block, or refine the
-    // mixed-precision subspace once its residuals look converged
-    bool refine = !exact && (small || force_refine);
+    // Mixed precision: FP32 sigma for new directions while the exact
+    // (refined) residual keeps improving; once it stalls near the FP32 noise
+    // floor, or gets close to the target, switch to FP64 directions.
+    if (phase32 && exact && just_refined) {
+      if (maxr < 4.0 * switch_tol || maxr > 0.5 * last_refined) phase32 = false;
+      last_refined = maxr;
+    }
+    just_refined = false;
+    bool refine = !exact && (!phase32 || maxr < switch_tol || force_refine);
     bool need_restart = (m + k > mmax) || refine;
     force_refine = false;
     if (need_restart) {
@@ -319,10 +328,11 @@ pq_status ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *ener
       PQ_CUBLAS_TRY(cublasDgemm(D.cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, r, m, &one, D.V.as<double>(), (int)n,
                                 D.tmp.as<double>(), m, &zero, D.T.as<double>(), (int)n));
       PQ_CUDA_TRY(cudaMemcpyAsync(D.V.ptr, D.T.ptr, sizeof(double) * n * r, cudaMemcpyDeviceToDevice, st));
-      if (p->precision == PQ_FP32) {
-        // FP64 refinement: exact sigma of the restart vectors
+      if (!exact) {
+        // FP64 residual refinement: exact sigma of the restart vectors
         PQ_TRY(D.sigma(D.V.as<double>(), D.W.as<double>(), r, PQ_FP64, 0.0, &rep));
         exact = true;
+        just_refined = true;
       } else {
         PQ_CUBLAS_TRY(cublasDgemm(D.cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, r, m, &one, D.W.as<double>(), (int)n,
                                   D.tmp.as<double>(), m, &zero, D.T.as<double>(), (int)n));
@@ -357,9 +367,9 @@ pq_status ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *ener
       continue;
     }
     shift = theta[0];
-    PQ_TRY(D.sigma(D.V.as<double>() + (size_t)m * n, D.W.as<double>() + (size_t)m * n, added, p->precision, shift,
-                   &rep));
-    if (p->precision == PQ_FP32) exact = false;
+    const int prec = phase32 ? PQ_FP32 : PQ_FP64;
+    PQ_TRY(D.sigma(D.V.as<double>() + (size_t)m * n, D.W.as<double>() + (size_t)m * n, added, prec, shift, &rep));
+    if (prec == PQ_FP32) exact = false;
     m += added;
   }
   rep.iterations = std::min(it, iter_max);
