@@ -104,6 +104,21 @@ pq_status pq_ci_sigma(pq_ci_handle *h, const double *C, int64_t ldc, int32_t nve
 pq_status pq_ci_sigma_host(pq_ci_handle *h, const double *C, int64_t ldc, int32_t nvec, double *S, int64_t lds,
                            int32_t precision);
 
+/* Same as pq_ci_sigma, but allocates nothing: no reference counterpart (the
+ * reference's operator* allocates its result on every call).  For callers
+ * that may not call cudaMalloc/cudaFree while computing (a host whose device
+ * memory is pre-reserved by its own pool, a latency-critical loop that must
+ * not hit the implicit synchronisation of cudaMalloc/cudaFree, an iteration
+ * recorded into a CUDA graph).  The work vectors live in a fixed 2 x 16 MiB
+ * array compiled into the library, so n_dets * w * sizeof(T) must not exceed
+ * 16 MiB, where w = 4 for nvec >= 3 (else nvec) and T is double (PQ_FP64) or
+ * float (PQ_FP32); larger problems return PQ_ERR_ARG.  The array's device
+ * address is looked up on the first call on each device (make that call
+ * before any stream capture).  All calls share the array: calls that overlap
+ * on the GPU race and must be serialised by the caller. */
+pq_status pq_ci_sigma_noalloc(pq_ci_handle *h, const double *C, int64_t ldc, int32_t nvec, double *S, int64_t lds,
+                              int32_t precision);
+
 /* Native-layout sigma on DEVICE buffers interleaved by determinant:
  * X[det * nvec + v].  T = double (precision PQ_FP64) or float (PQ_FP32).
  * diag_shift is subtracted from H_II (sigma = (H - shift*1) X). */

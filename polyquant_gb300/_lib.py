@@ -18,7 +18,8 @@ PQ_XFORM_FP64, PQ_XFORM_BF16X3, PQ_XFORM_TF32X3 = 0, 1, 2
 
 EXPORTS = [
     "pq_last_error", "pq_version", "pq_ci_create", "pq_ci_destroy", "pq_ci_num_dets", "pq_ci_strings",
-    "pq_ci_det_unfold", "pq_ci_diag", "pq_ci_sigma", "pq_ci_sigma_host", "pq_ci_sigma_interleaved",
+    "pq_ci_det_unfold", "pq_ci_diag", "pq_ci_sigma", "pq_ci_sigma_host", "pq_ci_sigma_noalloc",
+    "pq_ci_sigma_interleaved",
     "pq_ci_davidson", "pq_ao2mo", "pq_mo1",
 ]
 
@@ -96,7 +97,7 @@ def load(path: str = LIB_PATH):
     L.pq_ci_det_unfold.argtypes = [P, P]
     L.pq_ci_diag.restype = I32
     L.pq_ci_diag.argtypes = [P, P]
-    for f in (L.pq_ci_sigma, L.pq_ci_sigma_host):
+    for f in (L.pq_ci_sigma, L.pq_ci_sigma_host, L.pq_ci_sigma_noalloc):
         f.restype = I32
         f.argtypes = [P, P, I64, I32, P, I64, I32]
     L.pq_ci_sigma_interleaved.restype = I32
