@@ -105,11 +105,21 @@ template <typename T, int NV> __device__ __forceinline__ void fma_vec(T (&acc)[N
   for (int v = 0; v < NV; v++) acc[v] = fma(c, x[v], acc[v]);
 }
 
+// v or -v selected by the low bit of `neg`, on the integer pipe
+__device__ __forceinline__ float flip_sign(float v, uint32_t neg) { return __int_as_float(__float_as_int(v) ^ (int)(neg << 31)); }
+__device__ __forceinline__ double flip_sign(double v, uint32_t neg) {
+  return __hiloint2double(__double2hiint(v) ^ (int)(neg << 31), __double2loint(v));
+}
+
 constexpr int SIGMA_THREADS = 256;
 constexpr int SIGMA_CHUNK = 8;
 
-template <typename T, int NV, bool FULL, bool TAB>
-__global__ void __launch_bounds__(SIGMA_THREADS) sigma_one_species_kernel(SigmaArgs<T> p) {
+// PK > 0: the thread's beta singles (J << 10 | pair << 1 | phase bit) are held
+// in PK registers and the alpha-beta loop runs alpha-neighbour-outer, so all
+// CTAs of one alpha string sweep the same rows of C at the same time (the L2
+// working set stays small).  Needs TAB, J < 2^22, pair < 512, <= PK singles.
+template <typename T, int NV, bool FULL, bool TAB, int PK>
+__global__ void __launch_bounds__(SIGMA_THREADS, (PK > 0 ? 2 : 1)) sigma_one_species_kernel(SigmaArgs<T> p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *Wa = reinterpret_cast<T *>(smem_raw);
   T *Jrow = Wa + p.npair;
@@ -206,40 +216,64 @@ __global__ void __launch_bounds__(SIGMA_THREADS) sigma_one_species_kernel(SigmaA
     }
   }
   // alpha-beta doubles: sign_a sign_b (pair_a | pair_b)_ab
-  for (int64_t j0 = b1_0; j0 < b1_1; j0 += SIGMA_CHUNK) {
-    int Jb[SIGMA_CHUNK], pb[SIGMA_CHUNK];
-    T sb[SIGMA_CHUNK];
+  if constexpr (PK > 0) {
+    uint32_t bpk[PK];
+    const int nb1 = (int)(b1_1 - b1_0);
 #pragma unroll
-    for (int c = 0; c < SIGMA_CHUNK; c++) {
-      if (j0 + c < b1_1) {
-        Jb[c] = __ldg(p.b.s1_J + j0 + c);
-        int info = __ldg(p.b.s1_info + j0 + c);
-        pb[c] = info >> 1;
-        sb[c] = (info & 1) ? T(-1) : T(1);
-      } else {
-        Jb[c] = 0x7fffffff;  // never below any row length
-        pb[c] = 0;
-        sb[c] = 0;
-      }
-    }
+    for (int c = 0; c < PK; c++)
+      bpk[c] = c < nb1 ? (((uint32_t)__ldg(p.b.s1_J + b1_0 + c) << 10) | (uint32_t)__ldg(p.b.s1_info + b1_0 + c))
+                       : 0xffffffffu;
     for (int e = 0; e < na1; e++) {
       const int Ja = __ldg(p.a.s1_J + a1_0 + e);
       const int64_t ro = __ldg(p.rowoff + Ja);
       const int la = FULL ? 0x7fffffff : __ldg(p.rowlen + Ja);
-      const T *row;
-      T sa = T(1);
-      if (TAB) {
-        row = Tab + e * npair;
-      } else {
-        const int info = __ldg(p.a.s1_info + a1_0 + e);
-        row = p.eab + (int64_t)(info >> 1) * npair;
-        sa = (info & 1) ? T(-1) : T(1);
+      const T *row = Tab + e * npair;
+#pragma unroll
+      for (int c = 0; c < PK; c++) {
+        const uint32_t w = bpk[c];
+        const int Jb = (int)(w >> 10);
+        if (c < nb1 && (FULL || Jb < la)) {
+          const T coef = flip_sign(row[(w >> 1) & 511u], w & 1u);
+          fma_vec<T, NV>(acc, coef, p.X + (ro + Jb) * NV);
+        }
       }
+    }
+  } else {
+    for (int64_t j0 = b1_0; j0 < b1_1; j0 += SIGMA_CHUNK) {
+      int Jb[SIGMA_CHUNK], pb[SIGMA_CHUNK];
+      uint32_t sb[SIGMA_CHUNK];
 #pragma unroll
       for (int c = 0; c < SIGMA_CHUNK; c++) {
-        if (Jb[c] < la) {
-          const T coef = (TAB ? row[pb[c]] : __ldg(row + pb[c]) * sa) * sb[c];
-          fma_vec<T, NV>(acc, coef, p.X + (ro + Jb[c]) * NV);
+        if (j0 + c < b1_1) {
+          Jb[c] = __ldg(p.b.s1_J + j0 + c);
+          int info = __ldg(p.b.s1_info + j0 + c);
+          pb[c] = info >> 1;
+          sb[c] = (uint32_t)(info & 1);
+        } else {
+          Jb[c] = 0x7fffffff;  // never below any row length
+          pb[c] = 0;
+          sb[c] = 0;
+        }
+      }
+      for (int e = 0; e < na1; e++) {
+        const int Ja = __ldg(p.a.s1_J + a1_0 + e);
+        const int64_t ro = __ldg(p.rowoff + Ja);
+        const int la = FULL ? 0x7fffffff : __ldg(p.rowlen + Ja);
+        const T *row;
+        uint32_t sa = 0;
+        if (TAB) {
+          row = Tab + e * npair;
+        } else {
+          const int info = __ldg(p.a.s1_info + a1_0 + e);
+          row = p.eab + (int64_t)(info >> 1) * npair;
+          sa = (uint32_t)(info & 1);
+        }
+#pragma unroll
+        for (int c = 0; c < SIGMA_CHUNK; c++) {
+          if (Jb[c] < la) {
+            const T coef = flip_sign(TAB ? row[pb[c]] : __ldg(row + pb[c]), sa ^ sb[c]);
+            fma_vec<T, NV>(acc, coef, p.X + (ro + Jb[c]) * NV);
+          }
         }
       }
     }
@@ -258,9 +292,9 @@ template <> SpinView<float> make_view<float>(const SpinTablesDev &t) {
           t.s1_F32.as<float>(), t.s2_off.as<int64_t>(), t.s2_J.as<int32_t>(), t.s2_D32.as<float>()};
 }
 
-template <typename T, int NV, bool FULL, bool TAB>
+template <typename T, int NV, bool FULL, bool TAB, int PK>
 static pq_status launch_sigma(const SigmaArgs<T> &a, int64_t na, size_t smem, cudaStream_t st) {
-  auto kern = sigma_one_species_kernel<T, NV, FULL, TAB>;
+  auto kern = sigma_one_species_kernel<T, NV, FULL, TAB, PK>;
   if (smem > 48 * 1024) PQ_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int64_t grid = na * a.nblk_b;
   if (grid > 0x7fffffffLL) {
@@ -298,10 +332,18 @@ static pq_status sigma_dispatch(pq_ci_handle *h, const T *X, T *Y, double shift)
     return PQ_ERR_ARG;
   }
   cudaStream_t st = h->stream;
+  // packed-register alpha-beta path when the beta singles fit the encoding
+  const int max1b = h->tab[0][1].max1;
+  const bool pack_ok = use_tab && nb < (1 << 22) && a.npair <= 511;
+  const int pk = !pack_ok ? 0 : (max1b <= 32 ? 32 : (max1b <= 64 ? 64 : 0));
   if (h->full) {
-    return use_tab ? launch_sigma<T, NV, true, true>(a, na, smem, st) : launch_sigma<T, NV, true, false>(a, na, smem, st);
+    if (pk == 32) return launch_sigma<T, NV, true, true, 32>(a, na, smem, st);
+    if (pk == 64) return launch_sigma<T, NV, true, true, 64>(a, na, smem, st);
+    return use_tab ? launch_sigma<T, NV, true, true, 0>(a, na, smem, st) : launch_sigma<T, NV, true, false, 0>(a, na, smem, st);
   }
-  return use_tab ? launch_sigma<T, NV, false, true>(a, na, smem, st) : launch_sigma<T, NV, false, false>(a, na, smem, st);
+  if (pk == 32) return launch_sigma<T, NV, false, true, 32>(a, na, smem, st);
+  if (pk == 64) return launch_sigma<T, NV, false, true, 64>(a, na, smem, st);
+  return use_tab ? launch_sigma<T, NV, false, true, 0>(a, na, smem, st) : launch_sigma<T, NV, false, false, 0>(a, na, smem, st);
 }
 
 pq_status ci_sigma_il(pq_ci_handle *h, const void *X, void *Y, int nvp, int precision, double shift) {

@@ -35,12 +35,14 @@ def _cases(h2o):
         "cisdt_9o_4a4b": synthetic_fci(9, 4, 4, seed=13, ex=[3, 3, 3]),
         "unrestricted_7o_3a2b": synthetic_unrestricted(7, 3, 2, seed=14),
         "one_electron_6o": synthetic_fci(6, 1, 0, seed=15),
+        # 595 orbital pairs and 93 singles per string: generic (unpacked) path, ERIs read from global
+        "cisd_34o_3a3b": synthetic_fci(34, 3, 3, seed=16, ex=[2, 2, 2]),
     }
     return out
 
 
 CASES = ["h2o_cis", "h2o_cisd", "h2o_fci", "fci_8o_4a3b", "cisd_10o_5a5b", "cisdt_9o_4a4b",
-         "unrestricted_7o_3a2b", "one_electron_6o"]
+         "unrestricted_7o_3a2b", "one_electron_6o", "cisd_34o_3a3b"]
 
 
 @pytest.fixture(scope="module")
