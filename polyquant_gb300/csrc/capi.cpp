@@ -102,6 +102,7 @@ pq_status pq_ci_det_unfold(const pq_ci_handle *h, int32_t *out) {
     set_error("pq_ci_det_unfold: NULL argument");
     return PQ_ERR_ARG;
   }
+  if (h->n_species == 2) return ci_unfold2(h, out);
   int64_t k = 0;
   for (size_t ia = 0; ia < h->rowlen.size(); ia++)
     for (int32_t ib = 0; ib < h->rowlen[ia]; ib++) {

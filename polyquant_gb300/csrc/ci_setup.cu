@@ -61,7 +61,7 @@ static bool next_comb(std::vector<int> &c, int n) {
   return true;
 }
 
-static pq_status make_strings(int n_orb, int n_e, int ex_max, std::vector<uint64_t> &out, std::vector<int32_t> &lvl) {
+pq_status make_strings(int n_orb, int n_e, int ex_max, std::vector<uint64_t> &out, std::vector<int32_t> &lvl) {
   out.clear();
   lvl.clear();
   uint64_t hf = 0;
@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(256) diag_kernel(int64_t nblk_b, const int64_t
 }
 
 // ---------------------------------------------------------------------------
-static pq_status build_spin_tables(pq_ci_handle *h, int s, int sp, const double *h1_host, const double *eri_host) {
+pq_status build_spin_tables(pq_ci_handle *h, int s, int sp, const double *h1_host, const double *eri_host) {
   cudaStream_t st = h->stream;
   SpinTablesDev &T = h->tab[s][sp];
   const std::vector<uint64_t> &masks = h->str[s][sp];
@@ -330,8 +330,9 @@ pq_status ci_build(pq_ci_handle *h) {
   const pq_ci_desc &d = h->desc;
   cudaStream_t st = h->stream;
   h->n_species = d.n_species;
+  if (d.n_species == 2) return ci_build2(h);
   if (d.n_species != 1) {
-    set_error("n_species=%d: this build handles one species", d.n_species);
+    set_error("n_species=%d: one or two species are supported", d.n_species);
     return PQ_ERR_ARG;
   }
   int maxorb = 0;

@@ -347,6 +347,7 @@ static pq_status sigma_dispatch(pq_ci_handle *h, const T *X, T *Y, double shift)
 }
 
 pq_status ci_sigma_il(pq_ci_handle *h, const void *X, void *Y, int nvp, int precision, double shift) {
+  if (h->n_species == 2) return ci_sigma2_il(h, X, Y, nvp, precision, shift);
   if (precision == PQ_FP64) {
     if (nvp == 1) return sigma_dispatch<double, 1>(h, (const double *)X, (double *)Y, shift);
     if (nvp == 2) return sigma_dispatch<double, 2>(h, (const double *)X, (double *)Y, shift);

@@ -94,11 +94,29 @@ struct pq_ci_handle {
   pq::DevBuf d_diag;
   // scratch for layout conversion
   pq::DevBuf x_il, y_il;
+  // two species: addressing of the product space (see ci_two.cu)
+  std::vector<int32_t> e_a, e_b;        // species-0 (alpha, beta) string pair of each kept pair ie
+  std::vector<int64_t> ebase;           // first determinant of pair ie's species-1 block
+  std::vector<int32_t> elev;            // allowed species-1 level of pair ie (-1: empty block)
+  int lcap = 0;
+  std::vector<int64_t> psize;           // species-1 block size per level
+  std::vector<int32_t> prowoff, prowlen;  // (lcap+1) x n_str[1][0]
+  std::vector<int64_t> pfirst;          // offset of level L's (a, b) list
+  std::vector<int32_t> pdet_a, pdet_b;  // species-1 (alpha, beta) of block entry q, per level
+  pq::DevBuf d_e_a, d_e_b, d_ebase, d_elev, d_prowoff, d_prowlen, d_pfirst, d_psize, d_pdet_a, d_pdet_b;
+  // integral blocks, row-major: [s] same-species alpha|beta, [se][sp] electron|positron
+  pq::DevBuf d_eabs64[2], d_eabs32[2], d_ep64[2][2], d_ep32[2][2];
 };
 
 namespace pq {
 // ci_setup.cu
 pq_status ci_build(pq_ci_handle *h);
+pq_status make_strings(int n_orb, int n_e, int ex_max, std::vector<uint64_t> &out, std::vector<int32_t> &lvl);
+pq_status build_spin_tables(pq_ci_handle *h, int s, int sp, const double *h1_host, const double *eri_host);
+// ci_two.cu (electron + positron product space)
+pq_status ci_build2(pq_ci_handle *h);
+pq_status ci_sigma2_il(pq_ci_handle *h, const void *X, void *Y, int nvp, int precision, double shift);
+pq_status ci_unfold2(const pq_ci_handle *h, int32_t *out);
 // ci_sigma.cu
 pq_status ci_sigma_il(pq_ci_handle *h, const void *X, void *Y, int nvec, int precision, double shift);
 pq_status ci_to_il(pq_ci_handle *h, const double *C, int64_t ldc, int v0, int nv, int nvp, int precision, void *X);
