@@ -1,10 +1,546 @@
-// Split-precision AO->MO transform on tcgen05 tensor cores (see ao2mo.cu for
-// the half-transform structure).
+// Split-precision AO->MO transform on the tcgen05 tensor cores.
+//
+// Same two pair-symmetric half transforms as the FP64 path (ao2mo.cu): for
+// each slice S (a symmetric n x n matrix: one ket AO pair in half 1, one bra MO
+// pair in half 2), T = C^T S C, written packed (i >= j).  Each slice costs two
+// GEMMs, both in the "A (M x K, K-major) times B (N x K, K-major)^T" form:
+//   GEMM 1:  U^T[m][nu] = sum_mu Ct[m][mu] S[nu][mu]    (A = C^T shared, B = S per slice)
+//   GEMM 2:  T[m][n]   = sum_nu U^T[m][nu] Ct[n][nu]    (A = U^T per slice, B = C^T shared)
+// Operands are split into a high and a low part (x = x_hi + x_lo) in BF16 or
+// TF32 and each product is formed as hi*hi + hi*lo + lo*hi with FP32
+// accumulation in tensor memory (three MMAs per K step).  BF16 and TF32 keep
+// FP32's 8-bit exponent, so no per-block scaling is needed for range.
+//
+// GEMM kernel: one CTA (128 threads) per 128 x 256 output tile.  Thread 0
+// issues TMA tile loads (128-byte swizzle, two stages of K = 128 bytes of
+// each of A_hi, A_lo, B_hi, B_lo) and the tcgen05.mma instructions; the
+// accumulator (128 lanes x 256 FP32 columns) lives in TMEM; all four warps
+// read it back with tcgen05.ld for the epilogue (BF16/TF32 split of the
+// result for the next GEMM, or the packed lower triangle).  Every mbarrier
+// wait is bounded; a wait that runs out records an error code and the kernel
+// winds down (waits, bounded again, for its own loads, frees TMEM, returns).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <vector>
+
 #include "pq_internal.h"
 
 namespace pq {
-pq_status ao2mo_tc(const double *, int, int64_t, const double *, int64_t, int64_t, int, double *, cudaStream_t) {
-  set_error("pq_ao2mo: split-precision tensor-core modes are not built yet");
-  return PQ_ERR_ARG;
+
+namespace tc {
+
+constexpr int BM = 128;          // output rows per CTA (TMEM lanes)
+constexpr int BN = 256;          // output columns per CTA (TMEM columns, UMMA N)
+constexpr int ROW_BYTES = 128;   // K extent of one stage, in bytes (one swizzle span)
+constexpr int STAGES = 2;
+constexpr int A_TILE = BM * ROW_BYTES;  // 16 KB
+constexpr int B_TILE = BN * ROW_BYTES;  // 32 KB
+constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
+
+enum { EPI_SPLIT = 0, EPI_PACK = 1 };
+enum { ERR_TIMEOUT_FULL = 1, ERR_TIMEOUT_MMA = 2, ERR_TIMEOUT_ACC = 3 };
+
+struct GemmArgs {
+  int M, N, K;                 // logical sizes
+  int m_tiles;                 // ceil(M / BM)
+  int a_batched, b_batched;    // operand varies with the batch index
+  int a_rows, b_rows;          // rows per batch in the operand tensors
+  int ld_out;                  // EPI_SPLIT: row length of the split output
+  void *out_hi, *out_lo;       // EPI_SPLIT outputs [b][M][ld_out]
+  float *out_pack;             // EPI_PACK output [b][M(M+1)/2]
+  int64_t pack_stride;         // elements per batch of out_pack
+  int *err;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
 }
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: true when the phase completed, false when the budget ran out
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try(bar, parity)) {
+    if (clock64() - t0 > WAIT_CYCLES) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// UMMA shared-memory descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);        // start address
+  d |= (uint64_t)1 << 16;                         // leading byte offset (unused for this layout)
+  d |= (uint64_t)(1024 >> 4) << 32;               // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;                         // descriptor version for tcgen05
+  d |= (uint64_t)2 << 61;                         // 128-byte swizzle
+  return d;
+}
+
+// instruction descriptor: D = F32, A/B format (1 = BF16 for kind::f16, 2 = TF32), K-major A and B
+__host__ __device__ constexpr uint32_t instr_desc(uint32_t ab_format) {
+  return (1u << 4) | (ab_format << 7) | (ab_format << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+
+template <bool TF32>
+__device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum) {
+  if constexpr (TF32) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accum)
+        : "memory");
+  } else {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accum)
+        : "memory");
+  }
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float tf32_round(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+// TF32 = operands stored as FP32 (tf32-rounded); otherwise BF16.
+template <bool TF32, int EPI>
+__global__ void __launch_bounds__(128, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant__ CUtensorMap tmA_lo,
+                   const __grid_constant__ CUtensorMap tmB_hi, const __grid_constant__ CUtensorMap tmB_lo, GemmArgs g) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1024-byte alignment of the shared-window address (128-byte swizzle atoms)
+  unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE_BYTES);
+  // bars[0..STAGES): tiles loaded; bars[STAGES..2*STAGES): MMAs of a stage done; bars[2*STAGES]: accumulator ready
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * STAGES + 1);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int b = blockIdx.x / g.m_tiles, mt = blockIdx.x % g.m_tiles;
+  constexpr int ESZ = TF32 ? 4 : 2;
+  constexpr int BK = ROW_BYTES / ESZ;         // K elements per stage
+  constexpr int UK = TF32 ? 8 : 16;           // K per MMA instruction
+  const int nst = (g.K + BK - 1) / BK;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < 2 * STAGES + 1; i++) mbar_init(smem_u32(bars + i), 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)), "r"(BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (threadIdx.x == 0) {
+    const int ya = (g.a_batched ? b * g.a_rows : 0) + mt * BM;
+    const int yb = g.b_batched ? b * g.b_rows : 0;
+    const uint32_t idesc = instr_desc(TF32 ? 2u : 1u);
+    int issued = 0;  // stages whose loads were issued
+    auto issue = [&](int s) {
+      const int buf = s % STAGES;
+      unsigned char *st = smem + buf * STAGE_BYTES;
+      const uint32_t bar = smem_u32(bars + buf);
+      mbar_expect_tx(bar, STAGE_BYTES);
+      const int x = s * BK;
+      tma_load_2d(smem_u32(st), &tmA_hi, x, ya, bar);
+      tma_load_2d(smem_u32(st + A_TILE), &tmA_lo, x, ya, bar);
+      tma_load_2d(smem_u32(st + 2 * A_TILE), &tmB_hi, x, yb, bar);
+      tma_load_2d(smem_u32(st + 2 * A_TILE + B_TILE), &tmB_lo, x, yb, bar);
+      issued = s + 1;
+    };
+    for (int s = 0; s < nst && s < STAGES; s++) issue(s);
+    bool ok = true;
+    for (int s = 0; s < nst && ok; s++) {
+      const int buf = s % STAGES;
+      const uint32_t par = (uint32_t)((s / STAGES) & 1);
+      if (!mbar_wait(smem_u32(bars + buf), par)) {
+        atomicCAS(g.err, 0, ERR_TIMEOUT_FULL);
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      unsigned char *st = smem + buf * STAGE_BYTES;
+      const uint32_t a_hi = smem_u32(st), a_lo = smem_u32(st + A_TILE);
+      const uint32_t b_hi = smem_u32(st + 2 * A_TILE), b_lo = smem_u32(st + 2 * A_TILE + B_TILE);
+#pragma unroll
+      for (int kk = 0; kk < BK / UK; kk++) {
+        const uint32_t off = kk * UK * ESZ;  // bytes along K inside the swizzle span
+        const uint32_t acc0 = (s > 0 || kk > 0) ? 1u : 0u;
+        mma<TF32>(tmem, smem_desc(a_hi + off), smem_desc(b_hi + off), idesc, acc0);
+        mma<TF32>(tmem, smem_desc(a_hi + off), smem_desc(b_lo + off), idesc, 1u);
+        mma<TF32>(tmem, smem_desc(a_lo + off), smem_desc(b_hi + off), idesc, 1u);
+      }
+      mma_commit(smem_u32(bars + STAGES + buf));
+      if (s + STAGES < nst) {
+        // the buffer is reloaded only after the MMAs reading it completed
+        if (!mbar_wait(smem_u32(bars + STAGES + buf), par)) {
+          atomicCAS(g.err, 0, ERR_TIMEOUT_MMA);
+          ok = false;
+          break;
+        }
+        issue(s + STAGES);
+      }
+    }
+    if (ok) {
+      mma_commit(smem_u32(bars + 2 * STAGES));
+    } else {
+      *abort_flag = 1;
+      // wind down: wait (bounded) for this CTA's own loads still in flight
+      for (int s = (issued > STAGES ? issued - STAGES : 0); s < issued; s++)
+        mbar_wait(smem_u32(bars + (s % STAGES)), (uint32_t)((s / STAGES) & 1));
+      mbar_try(smem_u32(bars + 2 * STAGES), 0);
+    }
+  }
+  __syncthreads();
+  bool acc_ok = (*abort_flag == 0);
+  if (acc_ok) {
+    acc_ok = mbar_wait(smem_u32(bars + 2 * STAGES), 0);
+    if (!acc_ok && lane == 0) atomicCAS(g.err, 0, ERR_TIMEOUT_ACC);
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+  if (acc_ok) {
+    const int row = mt * BM + warp * 32 + lane;  // output row of this thread (TMEM lane)
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      float v[32];
+      tmem_ld32(taddr + c0, v);
+      if (row >= g.M) continue;
+      if constexpr (EPI == EPI_SPLIT) {
+        if constexpr (TF32) {
+          float *hi = static_cast<float *>(g.out_hi) + ((int64_t)b * g.M + row) * g.ld_out;
+          float *lo = static_cast<float *>(g.out_lo) + ((int64_t)b * g.M + row) * g.ld_out;
+#pragma unroll
+          for (int i = 0; i < 32; i++) {
+            const int n = c0 + i;
+            if (n < g.N) {
+              const float h = tf32_round(v[i]);
+              hi[n] = h;
+              lo[n] = tf32_round(v[i] - h);
+            }
+          }
+        } else {
+          __nv_bfloat16 *hi = static_cast<__nv_bfloat16 *>(g.out_hi) + ((int64_t)b * g.M + row) * g.ld_out;
+          __nv_bfloat16 *lo = static_cast<__nv_bfloat16 *>(g.out_lo) + ((int64_t)b * g.M + row) * g.ld_out;
+#pragma unroll
+          for (int i = 0; i < 32; i++) {
+            const int n = c0 + i;
+            if (n < g.N) {
+              const __nv_bfloat16 h = __float2bfloat16_rn(v[i]);
+              hi[n] = h;
+              lo[n] = __float2bfloat16_rn(v[i] - __bfloat162float(h));
+            }
+          }
+        }
+      } else {
+        float *out = g.out_pack + (int64_t)b * g.pack_stride + (int64_t)row * (row + 1) / 2;
+#pragma unroll
+        for (int i = 0; i < 32; i++) {
+          const int n = c0 + i;
+          if (n <= row && n < g.N) out[n] = v[i];
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// operand preparation
+template <bool TF32> struct Split;
+template <> struct Split<false> {
+  using T = __nv_bfloat16;
+  static __device__ __forceinline__ void run(double x, T &h, T &l) {
+    h = __double2bfloat16(x);
+    l = __double2bfloat16(x - (double)__bfloat162float(h));
+  }
+};
+template <> struct Split<true> {
+  using T = float;
+  static __device__ __forceinline__ void run(double x, T &h, T &l) {
+    h = tf32_round((float)x);
+    l = tf32_round((float)(x - (double)h));
+  }
+};
+
+// Ct[m][mu] = C[mu + m*ldc], split, row length ld (>= n_ao)
+template <bool TF32>
+__global__ void split_ct_kernel(const double *C, int64_t ldc, int n_ao, int n_mo, int ld, typename Split<TF32>::T *hi,
+                                typename Split<TF32>::T *lo) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)n_mo * ld) return;
+  int m = (int)(i / ld), mu = (int)(i - (int64_t)m * ld);
+  double x = mu < n_ao ? C[mu + (int64_t)m * ldc] : 0.0;
+  Split<TF32>::run(x, hi[i], lo[i]);
+}
+
+__device__ __forceinline__ int64_t tri64(int64_t i, int64_t j) { return i > j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i; }
+
+// slice b of a pair-matrix source, split: S[b][nu][mu] = src(tri(mu,nu), b0 + b)
+// src64: column-major (ld x ncols) FP64 pair matrix (element (r, c) at r + c*ld)
+// src32: row-major FP32 pair rows (element (r, c) at c*ld + r), i.e. row c holds the slice
+template <bool TF32>
+__global__ void split_slices_kernel(const double *src64, const float *src32, int64_t ld, int n, int ld_row, int64_t b0,
+                                    int nb, typename Split<TF32>::T *hi, typename Split<TF32>::T *lo) {
+  const int64_t per = (int64_t)n * ld_row;
+  const int64_t total = per * nb;
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (; i < total; i += stride) {
+    int64_t b = i / per, r = i - b * per;
+    int nu = (int)(r / ld_row), mu = (int)(r - (int64_t)nu * ld_row);
+    double x = 0.0;
+    if (mu < n) {
+      int64_t pr = tri64(mu, nu), c = b0 + b;
+      x = src64 ? src64[pr + c * ld] : (double)src32[c * ld + pr];
+    }
+    Split<TF32>::run(x, hi[i], lo[i]);
+  }
+}
+
+// full column-major pair matrix from the 8-fold packed vector
+__global__ void expand_packed8_kernel(const double *packed, int64_t np, double *full) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (; i < np * np; i += stride) {
+    int64_t c = i / np, r = i - c * np;
+    full[i] = packed[tri64(r, c)];
+  }
+}
+
+// out[c*rows + r] = in[r*cols + c] (FP32 tiles), optionally widened to FP64
+template <typename TO>
+__global__ void transpose32_kernel(const float *in, int64_t rows, int64_t cols, TO *out) {
+  __shared__ float tile[32][33];
+  int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    int64_t r = r0 + y, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) tile[y][threadIdx.x] = in[r * cols + c];
+  }
+  __syncthreads();
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    int64_t c = c0 + y, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) out[c * rows + r] = (TO)tile[threadIdx.x][y];
+  }
+}
+
+}  // namespace tc
+
+// ---------------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+// 2-D tensor map over a row-major (rows x kdim) operand, box (BK x box_rows), 128-byte swizzle
+static pq_status make_map(CUtensorMap *m, const void *base, bool tf32, int64_t rows, int64_t kdim, int64_t ld,
+                          int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) {
+    set_error("cuTensorMapEncodeTiled is not available from the driver");
+    return PQ_ERR_CUDA;
+  }
+  const int esz = tf32 ? 4 : 2;
+  cuuint64_t dims[2] = {(cuuint64_t)kdim, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld * esz)};
+  cuuint32_t box[2] = {(cuuint32_t)(tc::ROW_BYTES / esz), (cuuint32_t)box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = fn(m, tf32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base),
+                  dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d): rows=%lld k=%lld ld=%lld", (int)r, (long long)rows, (long long)kdim,
+              (long long)ld);
+    return PQ_ERR_CUDA;
+  }
+  return PQ_OK;
+}
+
+struct Operand {
+  const void *hi, *lo;
+  int64_t rows;  // total rows in memory
+  int64_t ld;    // row length in elements
+};
+
+template <bool TF32, int EPI>
+static pq_status run_gemm(const Operand &A, const Operand &B, bool a_batched, bool b_batched, int M, int N, int K,
+                          int nbatch, const tc::GemmArgs &gin, cudaStream_t st) {
+  CUtensorMap ma_hi, ma_lo, mb_hi, mb_lo;
+  PQ_TRY(make_map(&ma_hi, A.hi, TF32, A.rows, K, A.ld, tc::BM));
+  PQ_TRY(make_map(&ma_lo, A.lo, TF32, A.rows, K, A.ld, tc::BM));
+  PQ_TRY(make_map(&mb_hi, B.hi, TF32, B.rows, K, B.ld, tc::BN));
+  PQ_TRY(make_map(&mb_lo, B.lo, TF32, B.rows, K, B.ld, tc::BN));
+  tc::GemmArgs g = gin;
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.m_tiles = (M + tc::BM - 1) / tc::BM;
+  g.a_batched = a_batched;
+  g.b_batched = b_batched;
+  g.a_rows = M;
+  g.b_rows = N;
+  auto kern = tc::tc_gemm_kernel<TF32, EPI>;
+  PQ_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES));
+  const int64_t grid = (int64_t)nbatch * g.m_tiles;
+  kern<<<(unsigned)grid, 128, tc::SMEM_BYTES, st>>>(ma_hi, ma_lo, mb_hi, mb_lo, g);
+  PQ_CUDA_TRY(cudaGetLastError());
+  return PQ_OK;
+}
+
+template <bool TF32>
+static pq_status ao2mo_tc_impl(const double *eri_ao, int layout, int64_t n, const double *C, int64_t ldc, int64_t nm,
+                               double *eri_mo, cudaStream_t st) {
+  using E = typename tc::Split<TF32>::T;
+  const int64_t npa = n * (n + 1) / 2, npm = nm * (nm + 1) / 2;
+  const int ld = (int)((n + 7) / 8 * 8);    // AO row length (16-byte rows for TMA)
+  DevBuf full, cth, ctl, sh, sl, uh, ul, H1, H1t, Erow, err;
+  const double *pairs = eri_ao;
+  if (layout == PQ_AO_PACKED8) {
+    PQ_TRY(full.alloc(sizeof(double) * npa * npa));
+    tc::expand_packed8_kernel<<<152 * 32, 256, 0, st>>>(eri_ao, npa, full.as<double>());
+    PQ_CUDA_TRY(cudaGetLastError());
+    pairs = full.as<double>();
+  }
+  PQ_TRY(err.alloc(sizeof(int)));
+  PQ_CUDA_TRY(cudaMemsetAsync(err.ptr, 0, sizeof(int), st));
+  // C^T split, rows = MO, row length ld (AO)
+  PQ_TRY(cth.alloc(sizeof(E) * nm * ld));
+  PQ_TRY(ctl.alloc(sizeof(E) * nm * ld));
+  tc::split_ct_kernel<TF32><<<(unsigned)((nm * ld + 255) / 256), 256, 0, st>>>(C, ldc, (int)n, (int)nm, ld, cth.as<E>(),
+                                                                               ctl.as<E>());
+  PQ_CUDA_TRY(cudaGetLastError());
+  // slices per batch: S (n x ld) and U^T (nm x ld) in hi/lo
+  const int64_t bt = std::max<int64_t>(1, std::min<int64_t>(std::max(npa, npm), 4096));
+  PQ_TRY(sh.alloc(sizeof(E) * bt * n * ld));
+  PQ_TRY(sl.alloc(sizeof(E) * bt * n * ld));
+  PQ_TRY(uh.alloc(sizeof(E) * bt * nm * ld));
+  PQ_TRY(ul.alloc(sizeof(E) * bt * nm * ld));
+  PQ_TRY(H1.alloc(sizeof(float) * npa * npm));
+  tc::GemmArgs g{};
+  g.err = err.as<int>();
+  Operand ct{cth.ptr, ctl.ptr, nm, ld};
+  auto half = [&](const double *src64, const float *src32, int64_t ld_src, int64_t nslices, float *out) -> pq_status {
+    for (int64_t b0 = 0; b0 < nslices; b0 += bt) {
+      const int nb = (int)std::min(bt, nslices - b0);
+      tc::split_slices_kernel<TF32><<<152 * 32, 256, 0, st>>>(src64, src32, ld_src, (int)n, ld, b0, nb, sh.as<E>(),
+                                                              sl.as<E>());
+      PQ_CUDA_TRY(cudaGetLastError());
+      // GEMM 1: U^T[b] (nm x n) = Ct (nm x n) . S[b]^T, K = n
+      Operand S{sh.ptr, sl.ptr, (int64_t)nb * n, ld};
+      tc::GemmArgs g1 = g;
+      g1.out_hi = uh.ptr;
+      g1.out_lo = ul.ptr;
+      g1.ld_out = ld;
+      PQ_TRY((run_gemm<TF32, tc::EPI_SPLIT>(ct, S, false, true, (int)nm, (int)n, (int)n, nb, g1, st)));
+      // GEMM 2: T[b] (nm x nm) = U^T[b] . Ct^T, K = n; packed lower triangle
+      Operand U{uh.ptr, ul.ptr, (int64_t)nb * nm, ld};
+      tc::GemmArgs g2 = g;
+      g2.out_pack = out + b0 * npm;
+      g2.pack_stride = npm;
+      PQ_TRY((run_gemm<TF32, tc::EPI_PACK>(U, ct, true, false, (int)nm, (int)nm, (int)n, nb, g2, st)));
+    }
+    return PQ_OK;
+  };
+  // half 1 over AO ket pairs: H1[ket][ij]
+  PQ_TRY(half(pairs, nullptr, npa, npa, H1.as<float>()));
+  full.release();
+  // H1t[ij][ket]
+  PQ_TRY(H1t.alloc(sizeof(float) * npa * npm));
+  {
+    dim3 grid((unsigned)((npm + 31) / 32), (unsigned)((npa + 31) / 32));
+    if (grid.y > 65535) {
+      set_error("ao2mo: too many pairs for the transpose grid");
+      return PQ_ERR_ARG;
+    }
+    tc::transpose32_kernel<float><<<grid, dim3(32, 8), 0, st>>>(H1.as<float>(), npa, npm, H1t.as<float>());
+    PQ_CUDA_TRY(cudaGetLastError());
+  }
+  H1.release();
+  // half 2 over MO bra pairs: Erow[ij][kl]; slices read from rows of H1t (row ij holds the AO pair vector)
+  PQ_TRY(Erow.alloc(sizeof(float) * npm * npm));
+  PQ_TRY(half(nullptr, H1t.as<float>(), npa, npm, Erow.as<float>()));
+  H1t.release();
+  {
+    dim3 grid((unsigned)((npm + 31) / 32), (unsigned)((npm + 31) / 32));
+    tc::transpose32_kernel<double><<<grid, dim3(32, 8), 0, st>>>(Erow.as<float>(), npm, npm, eri_mo);
+    PQ_CUDA_TRY(cudaGetLastError());
+  }
+  int herr = 0;
+  PQ_CUDA_TRY(cudaMemcpyAsync(&herr, err.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+  PQ_CUDA_TRY(cudaStreamSynchronize(st));
+  if (herr) {
+    set_error("ao2mo tensor-core GEMM: bounded wait gave up (code %d)", herr);
+    return PQ_TIMEOUT;
+  }
+  return PQ_OK;
+}
+
+pq_status ao2mo_tc(const double *eri_ao, int layout, int64_t n_ao, const double *Ca, int64_t lda, int64_t nmo, int mode,
+                   double *eri_mo, cudaStream_t st) {
+  if (n_ao > tc::BN || nmo > tc::BN) {
+    set_error("pq_ao2mo: split-precision modes support n_ao, n_mo <= %d", tc::BN);
+    return PQ_ERR_ARG;
+  }
+  if (mode == PQ_XFORM_BF16X3) return ao2mo_tc_impl<false>(eri_ao, layout, n_ao, Ca, lda, nmo, eri_mo, st);
+  return ao2mo_tc_impl<true>(eri_ao, layout, n_ao, Ca, lda, nmo, eri_mo, st);
+}
+
 }  // namespace pq
