@@ -160,6 +160,82 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def peak_bf16():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        return float(json.load(open(path))["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
+
+
+def bench_ao2mo(n=256, L=1024, seed=0):
+    """AO->MO transform, N_AO = N_MO = 256: (mu nu|la si) = sum_L B_L,mu nu B_L,la si, 8-fold packed FP64 on the
+    device; C = Q of a seeded Gaussian.  Times the split-precision tensor-core modes and the FP64 path, and reports
+    the errors of the split modes against the FP64 result."""
+    import torch
+
+    from polyquant_gb300 import synthetic
+    from polyquant_gb300._lib import PQ_XFORM_BF16X3, PQ_XFORM_FP64, PQ_XFORM_TF32X3
+    from polyquant_gb300.integral import ao2mo
+
+    Bp = torch.from_numpy(synthetic.ao_eri_pairs(n, seed=seed, L=L)).cuda()
+    M = Bp.t() @ Bp
+    del Bp
+    npair = M.shape[0]
+    mask = torch.ones(npair, npair, dtype=torch.bool, device="cuda").tril_()
+    packed = torch.masked_select(M, mask)
+    del M, mask
+    C = torch.from_numpy(synthetic.mo_coefficients(n, n, seed=seed + 1)).cuda()
+    flops = 8.0 * npair * n ** 3  # two pair-symmetric half transforms (4 n^3 per slice each)
+    out = {}
+
+    def timed(mode, reps):
+        ao2mo(packed, C, mode=mode)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            r = ao2mo(packed, C, mode=mode)
+        e1.record()
+        torch.cuda.synchronize()
+        return r, e0.elapsed_time(e1) / reps
+
+    ref, ms64 = timed(PQ_XFORM_FP64, 1)
+    scale = ref.abs().max().item()
+    peak, src = peak_bf16()
+    for name, mode in (("bf16x3", PQ_XFORM_BF16X3), ("tf32x3", PQ_XFORM_TF32X3)):
+        r, ms = timed(mode, 3)
+        d = r - ref
+        tf = flops / (ms * 1e-3) / 1e12
+        out[name] = {"ms": ms, "tflops": tf, "max_abs_err": d.abs().max().item(),
+                     "rms_err": d.pow(2).mean().sqrt().item(), "max_abs_value": scale}
+        del r, d
+    out["fp64"] = {"ms": ms64, "tflops": flops / (ms64 * 1e-3) / 1e12}
+    b = out["bf16x3"]
+    return {"metric": "AO->MO TFLOP/s", "value": b["tflops"], "unit": "TFLOP/s", "mode": "bf16x3",
+            "workload": f"N_AO = N_MO = {n}, L = {L}, 8-fold packed FP64 input, seed {seed}",
+            "algorithmic_flops": flops, "modes": out,
+            "roofline": {"bound": "tensor", "achieved": b["tflops"], "peak": peak, "unit": "TFLOP/s",
+                         "frac": b["tflops"] / peak, "peak_source": src,
+                         "note": "algorithmic flops; the split modes issue 3 MMAs per product"}}
+
+
+def time_to_solution(ds, roots=4, nsub=8, tol=1e-4):
+    """Wall time of the FP64 and the mixed (FP32 sigma + FP64 refinement) Davidson to a residual that bounds the
+    energy error well below 1 uEh, with each energy's error against a tightly converged FP64 solve."""
+    from polyquant_gb300._lib import PQ_FP32, PQ_FP64
+
+    e_ref, i_ref = ds.davidson(num_states=roots, num_subspace_vec=nsub, convergence_E=1e-7, precision=PQ_FP64)
+    res = {"reference": {"energies": e_ref.tolist(), "seconds": i_ref["seconds"], "iterations": i_ref["iterations"],
+                         "residual": 1e-7}}
+    for name, prec in (("fp64", PQ_FP64), ("mixed", PQ_FP32)):
+        e, info = ds.davidson(num_states=roots, num_subspace_vec=nsub, convergence_E=tol, precision=prec)
+        res[name] = {"seconds": info["seconds"], "iterations": info["iterations"], "converged": info["converged"],
+                     "sigma_calls_fp64": info["sigma_calls_fp64"], "sigma_calls_fp32": info["sigma_calls_fp32"],
+                     "max_abs_energy_error": float(np.abs(e - e_ref).max()), "residual": tol}
+    res["speedup_mixed_vs_fp64"] = res["fp64"]["seconds"] / res["mixed"]["seconds"]
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -171,6 +247,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--norb", type=int, default=N_ORB, help="smaller FCI case for profiling only")
     ap.add_argument("--nel", type=int, default=N_A, help="electrons per spin of the profiling case")
+    ap.add_argument("--no-ao2mo", action="store_true")
+    ap.add_argument("--tts", action="store_true", help="also measure time to 1 uEh (FP64 vs mixed Davidson)")
     args = ap.parse_args()
     globals().update(N_ORB=args.norb, N_A=args.nel, N_B=args.nel)
 
@@ -265,6 +343,16 @@ def main():
         e2e = {"value": units / dt, "unit": UNIT, "h2d_bytes_per_step": n * ROOTS * 8, "d2h_bytes_per_step": n * ROOTS * 8,
                "ms_per_step": dt * 1e3, "rel_diff_vs_device": err}
 
+    tts = None
+    if args.tts:
+        tts = time_to_solution(ds, roots=ROOTS)
+    ao = None
+    if not args.no_ao2mo and rank == 0:
+        del X64, Y64, X32, Y32
+        ds.close()
+        torch.cuda.empty_cache()
+        ao = bench_ao2mo()
+
     cb = None
     if rank == 0 and not args.no_cpu:
         cb = cpu_baseline(budget_s=args.cpu_budget)
@@ -283,6 +371,8 @@ def main():
                              "algorithmic_bytes_per_launch": bytes_alg},
                 "gpu_launches": args.steps,
                 "clocks": clk.summary(),
+                "ao2mo": ao,
+                "time_to_1uEh": tts,
                 "cpu_baseline": cb}
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -318,7 +318,9 @@ pq_status ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *ener
     bool need_restart = (m + k > mmax) || refine;
     force_refine = false;
     if (need_restart) {
-      int r = refine ? k : std::min(m0, m);
+      // mixed precision restarts keep only the Ritz vectors: each refinement
+      // is then one FP64 sigma call for the k roots
+      int r = (refine || p->precision == PQ_FP32) ? k : std::min(m0, m);
       r = std::max(r, k);
       // V[:, 0:r] = V Z[:, 0:r]; W likewise (via the temporary T)
       PQ_TRY(D.tmp.ensure(sizeof(double) * (size_t)m * r));
