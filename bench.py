@@ -248,6 +248,7 @@ def main():
     ap.add_argument("--norb", type=int, default=N_ORB, help="smaller FCI case for profiling only")
     ap.add_argument("--nel", type=int, default=N_A, help="electrons per spin of the profiling case")
     ap.add_argument("--no-ao2mo", action="store_true")
+    ap.add_argument("--only-ao2mo", action="store_true", help="run only the AO->MO measurement (profiling case)")
     ap.add_argument("--tts", action="store_true", help="also measure time to 1 uEh (FP64 vs mixed Davidson)")
     args = ap.parse_args()
     globals().update(N_ORB=args.norb, N_A=args.nel, N_B=args.nel)
@@ -261,6 +262,9 @@ def main():
 
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
+    if args.only_ao2mo:
+        print(json.dumps(bench_ao2mo()), flush=True)
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist

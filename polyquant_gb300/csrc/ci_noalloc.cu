@@ -91,7 +91,7 @@ extern "C" pq_status pq_ci_sigma_noalloc(pq_ci_handle *h, const double *C, int64
     int nv = nvec - v0 < 4 ? nvec - v0 : 4;
     int nvp = nv == 1 ? 1 : (nv == 2 ? 2 : 4);
     PQ_TRY(ci_to_il(h, C, ldc, v0, nv, nvp, precision, X));
-    PQ_TRY(ci_sigma_il(h, X, Y, nvp, precision, 0.0));
+    PQ_TRY(ci_sigma_il(h, X, Y, nvp, precision, 0.0, /*allow_scratch=*/false));
     PQ_TRY(ci_from_il(h, Y, v0, nv, nvp, precision, S, lds));
   }
   return PQ_OK;

@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 
@@ -394,6 +395,10 @@ pq_status ci_build(pq_ci_handle *h) {
   PQ_TRY(upload(h->d_eab64, eab_rm, st));
   std::vector<float> eab32(eab_rm.begin(), eab_rm.end());
   PQ_TRY(upload(h->d_eab32, eab32, st));
+  std::vector<float> eba32((size_t)npair * npair);
+  for (int r = 0; r < npair; r++)
+    for (int c = 0; c < npair; c++) eba32[(size_t)c * npair + r] = eab32[(size_t)r * npair + c];
+  PQ_TRY(upload(h->d_eba32, eba32, st));
   // diagonal
   PQ_TRY(h->d_diag.alloc(sizeof(double) * (h->n_dets + 1)));
   int64_t nblk_b = (nb + 255) / 256;
@@ -406,6 +411,7 @@ pq_status ci_build(pq_ci_handle *h) {
     PQ_CUDA_TRY(cudaGetLastError());
   }
   PQ_CUDA_TRY(cudaStreamSynchronize(st));
+  h->fp32_v2 = sigma32_v2_applicable(h) && getenv("PQ_SIGMA32_GATHER") == nullptr;
   return PQ_OK;
 }
 

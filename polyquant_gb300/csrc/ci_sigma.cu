@@ -346,8 +346,10 @@ static pq_status sigma_dispatch(pq_ci_handle *h, const T *X, T *Y, double shift)
   return use_tab ? launch_sigma<T, NV, false, true, 0>(a, na, smem, st) : launch_sigma<T, NV, false, false, 0>(a, na, smem, st);
 }
 
-pq_status ci_sigma_il(pq_ci_handle *h, const void *X, void *Y, int nvp, int precision, double shift) {
+pq_status ci_sigma_il(pq_ci_handle *h, const void *X, void *Y, int nvp, int precision, double shift,
+                      bool allow_scratch) {
   if (h->n_species == 2) return ci_sigma2_il(h, X, Y, nvp, precision, shift);
+  if (precision == PQ_FP32 && allow_scratch && h->fp32_v2) return ci_sigma32_v2(h, X, Y, nvp, shift);
   if (precision == PQ_FP64) {
     if (nvp == 1) return sigma_dispatch<double, 1>(h, (const double *)X, (double *)Y, shift);
     if (nvp == 2) return sigma_dispatch<double, 2>(h, (const double *)X, (double *)Y, shift);

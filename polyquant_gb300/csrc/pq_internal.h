@@ -94,6 +94,9 @@ struct pq_ci_handle {
   pq::DevBuf d_diag;
   // scratch for layout conversion
   pq::DevBuf x_il, y_il;
+  // scratch of the FP32 full-CI sigma (transposed copies) and the transposed cross block
+  pq::DevBuf x_t, z_t, d_eba32;
+  bool fp32_v2 = false;  // FP32 sigma uses ci_sigma32.cu
   // two species: addressing of the product space (see ci_two.cu)
   std::vector<int32_t> e_a, e_b;        // species-0 (alpha, beta) string pair of each kept pair ie
   std::vector<int64_t> ebase;           // first determinant of pair ie's species-1 block
@@ -118,7 +121,12 @@ pq_status ci_build2(pq_ci_handle *h);
 pq_status ci_sigma2_il(pq_ci_handle *h, const void *X, void *Y, int nvp, int precision, double shift);
 pq_status ci_unfold2(const pq_ci_handle *h, int32_t *out);
 // ci_sigma.cu
-pq_status ci_sigma_il(pq_ci_handle *h, const void *X, void *Y, int nvec, int precision, double shift);
+// allow_scratch = false keeps sigma on kernels that need no work memory beyond X and Y
+pq_status ci_sigma_il(pq_ci_handle *h, const void *X, void *Y, int nvec, int precision, double shift,
+                      bool allow_scratch = true);
+// ci_sigma32.cu
+bool sigma32_v2_applicable(const pq_ci_handle *h);
+pq_status ci_sigma32_v2(pq_ci_handle *h, const void *X, void *Y, int nvp, double shift);
 pq_status ci_to_il(pq_ci_handle *h, const double *C, int64_t ldc, int v0, int nv, int nvp, int precision, void *X);
 pq_status ci_from_il(pq_ci_handle *h, const void *Y, int v0, int nv, int nvp, int precision, double *S, int64_t lds);
 // ci_davidson.cu

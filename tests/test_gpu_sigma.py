@@ -133,6 +133,20 @@ def test_sigma_properties_medium():
     assert np.abs(HX.cpu().numpy()[rows] - S_rows).max() <= SIGMA_RTOL_FP64 * np.abs(S_rows).max()
 
 
+def test_sigma_fp32_full_ci_medium():
+    """FP32 sigma of a full-CI space (transposed same-spin passes + alpha-beta scatter) against FP64."""
+    from polyquant_gb300._lib import PQ_FP32
+
+    p = synthetic_fci(12, 6, 6, seed=22)
+    g = gpu_detset(p)
+    gen = torch.Generator(device="cuda").manual_seed(6)
+    for k in (1, 2, 4):
+        X = torch.randn(g.N_dets, k, device="cuda", dtype=torch.float64, generator=gen)
+        S64 = g.sigma(X)
+        S32 = g.sigma(X, precision=PQ_FP32)
+        assert (S32 - S64).abs().max().item() <= SIGMA_RTOL_FP32 * S64.abs().max().item()
+
+
 def test_davidson_h2o_energies(cases, h2o):
     """H2O/STO-3G CISD energies (calculation_test.cpp:253-260) and FCI vs the oracle's dense H."""
     r = h2o("library")
