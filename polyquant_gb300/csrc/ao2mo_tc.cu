@@ -40,6 +40,8 @@ constexpr int A_TILE = BM * ROW_BYTES;  // 16 KB
 constexpr int B_TILE = BN * ROW_BYTES;  // 32 KB
 constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+constexpr int TILE_LD = BN + 1;  // epilogue staging row stride (floats)
+static_assert(BM * TILE_LD * 4 <= STAGES * STAGE_BYTES, "epilogue tile must fit the stage buffers");
 constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
 
 enum { EPI_SPLIT = 0, EPI_PACK = 1 };
@@ -248,46 +250,43 @@ __global__ void __launch_bounds__(128, 1)
   }
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
+  // Epilogue: TMEM -> shared tile (the stage buffers are idle once every MMA
+  // has completed) -> coalesced row stores by the whole CTA.
+  float *tile = reinterpret_cast<float *>(smem);  // BM x TILE_LD floats (odd stride: conflict-free column writes)
   if (acc_ok) {
-    const int row = mt * BM + warp * 32 + lane;  // output row of this thread (TMEM lane)
+    const int r = warp * 32 + lane;
     const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
     for (int c0 = 0; c0 < BN; c0 += 32) {
       float v[32];
       tmem_ld32(taddr + c0, v);
-      if (row >= g.M) continue;
+#pragma unroll
+      for (int i = 0; i < 32; i++) tile[r * TILE_LD + c0 + i] = v[i];
+    }
+  }
+  __syncthreads();
+  if (acc_ok) {
+    for (int r = 0; r < BM; r++) {
+      const int m = mt * BM + r;
+      if (m >= g.M) break;
+      const float *trow = tile + r * TILE_LD;
       if constexpr (EPI == EPI_SPLIT) {
-        if constexpr (TF32) {
-          float *hi = static_cast<float *>(g.out_hi) + ((int64_t)b * g.M + row) * g.ld_out;
-          float *lo = static_cast<float *>(g.out_lo) + ((int64_t)b * g.M + row) * g.ld_out;
-#pragma unroll
-          for (int i = 0; i < 32; i++) {
-            const int n = c0 + i;
-            if (n < g.N) {
-              const float h = tf32_round(v[i]);
-              hi[n] = h;
-              lo[n] = tf32_round(v[i] - h);
-            }
-          }
-        } else {
-          __nv_bfloat16 *hi = static_cast<__nv_bfloat16 *>(g.out_hi) + ((int64_t)b * g.M + row) * g.ld_out;
-          __nv_bfloat16 *lo = static_cast<__nv_bfloat16 *>(g.out_lo) + ((int64_t)b * g.M + row) * g.ld_out;
-#pragma unroll
-          for (int i = 0; i < 32; i++) {
-            const int n = c0 + i;
-            if (n < g.N) {
-              const __nv_bfloat16 h = __float2bfloat16_rn(v[i]);
-              hi[n] = h;
-              lo[n] = __float2bfloat16_rn(v[i] - __bfloat162float(h));
-            }
+        const int64_t base = ((int64_t)b * g.M + m) * g.ld_out;
+        for (int n = threadIdx.x; n < g.N; n += 128) {
+          const float x = trow[n];
+          if constexpr (TF32) {
+            const float h = tf32_round(x);
+            static_cast<float *>(g.out_hi)[base + n] = h;
+            static_cast<float *>(g.out_lo)[base + n] = tf32_round(x - h);
+          } else {
+            const __nv_bfloat16 h = __float2bfloat16_rn(x);
+            static_cast<__nv_bfloat16 *>(g.out_hi)[base + n] = h;
+            static_cast<__nv_bfloat16 *>(g.out_lo)[base + n] = __float2bfloat16_rn(x - __bfloat162float(h));
           }
         }
       } else {
-        float *out = g.out_pack + (int64_t)b * g.pack_stride + (int64_t)row * (row + 1) / 2;
-#pragma unroll
-        for (int i = 0; i < 32; i++) {
-          const int n = c0 + i;
-          if (n <= row && n < g.N) out[n] = v[i];
-        }
+        float *out = g.out_pack + (int64_t)b * g.pack_stride + (int64_t)m * (m + 1) / 2;
+        const int lim = m + 1 < g.N ? m + 1 : g.N;
+        for (int n = threadIdx.x; n < lim; n += 128) out[n] = trow[n];
       }
     }
   }
@@ -330,32 +329,60 @@ __device__ __forceinline__ int64_t tri64(int64_t i, int64_t j) { return i > j ? 
 // slice b of a pair-matrix source, split: S[b][nu][mu] = src(tri(mu,nu), b0 + b)
 // src64: column-major (ld x ncols) FP64 pair matrix (element (r, c) at r + c*ld)
 // src32: row-major FP32 pair rows (element (r, c) at c*ld + r), i.e. row c holds the slice
+// One block per slice; 32x32 tiles of the lower triangle are read with
+// consecutive pair indices (mu <= nu) and written to both triangles, the upper
+// one through a shared-memory transpose, so loads and stores are coalesced.
 template <bool TF32>
-__global__ void split_slices_kernel(const double *src64, const float *src32, int64_t ld, int n, int ld_row, int64_t b0,
-                                    int nb, typename Split<TF32>::T *hi, typename Split<TF32>::T *lo) {
-  const int64_t per = (int64_t)n * ld_row;
-  const int64_t total = per * nb;
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (; i < total; i += stride) {
-    int64_t b = i / per, r = i - b * per;
-    int nu = (int)(r / ld_row), mu = (int)(r - (int64_t)nu * ld_row);
-    double x = 0.0;
-    if (mu < n) {
-      int64_t pr = tri64(mu, nu), c = b0 + b;
-      x = src64 ? src64[pr + c * ld] : (double)src32[c * ld + pr];
+__global__ void __launch_bounds__(256) split_slices_kernel(const double *src64, const float *src32, int64_t ld, int n,
+                                                           int ld_row, int64_t b0, typename Split<TF32>::T *hi,
+                                                           typename Split<TF32>::T *lo) {
+  __shared__ double tile[32][33];
+  const int64_t b = blockIdx.x, c = b0 + b;
+  typename Split<TF32>::T *H = hi + b * (int64_t)n * ld_row, *L = lo + b * (int64_t)n * ld_row;
+  const int nt = (n + 31) / 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int tv = 0; tv < nt; tv++)
+    for (int tm = 0; tm <= tv; tm++) {
+      for (int y = ty; y < 32; y += 8) {
+        const int nu = tv * 32 + y, mu = tm * 32 + tx;
+        double x = 0.0;
+        if (nu < n && mu <= nu) {
+          const int64_t pr = (int64_t)nu * (nu + 1) / 2 + mu;
+          x = src64 ? src64[pr + c * ld] : (double)src32[c * ld + pr];
+          Split<TF32>::run(x, H[(int64_t)nu * ld_row + mu], L[(int64_t)nu * ld_row + mu]);
+        }
+        tile[y][tx] = x;
+      }
+      __syncthreads();
+      for (int y = ty; y < 32; y += 8) {
+        const int mu = tm * 32 + y, nu = tv * 32 + tx;
+        if (nu < n && mu < nu) Split<TF32>::run(tile[tx][y], H[(int64_t)mu * ld_row + nu], L[(int64_t)mu * ld_row + nu]);
+      }
+      __syncthreads();
     }
-    Split<TF32>::run(x, hi[i], lo[i]);
-  }
 }
 
-// full column-major pair matrix from the 8-fold packed vector
-__global__ void expand_packed8_kernel(const double *packed, int64_t np, double *full) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (; i < np * np; i += stride) {
-    int64_t c = i / np, r = i - c * np;
-    full[i] = packed[tri64(r, c)];
+// full column-major pair matrix from the 8-fold packed vector: one block per
+// 32x32 tile of the lower triangle (row tile >= column tile), read along
+// packed rows, written to both triangles through a shared-memory transpose
+__global__ void __launch_bounds__(256) expand_packed8_kernel(const double *packed, int64_t np, double *full) {
+  __shared__ double tile[32][33];
+  const int64_t tr = blockIdx.y, tcol = blockIdx.x;
+  if (tcol > tr) return;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int y = ty; y < 32; y += 8) {
+    const int64_t r = tr * 32 + y, c = tcol * 32 + tx;
+    double x = 0.0;
+    if (r < np && c <= r) {
+      x = packed[r * (r + 1) / 2 + c];
+      full[r * np + c] = x;  // element (c, r): column r, contiguous in c
+    }
+    tile[y][tx] = x;
+  }
+  __syncthreads();
+  for (int y = ty; y < 32; y += 8) {
+    const int64_t c = tcol * 32 + y, r = tr * 32 + tx;
+    if (r < np && c < r) full[c * np + r] = tile[tx][y];  // element (r, c): column c, contiguous in r
   }
 }
 
@@ -455,7 +482,12 @@ static pq_status ao2mo_tc_impl(const double *eri_ao, int layout, int64_t n, cons
   const double *pairs = eri_ao;
   if (layout == PQ_AO_PACKED8) {
     PQ_TRY(full.alloc(sizeof(double) * npa * npa));
-    tc::expand_packed8_kernel<<<152 * 32, 256, 0, st>>>(eri_ao, npa, full.as<double>());
+    const unsigned nt = (unsigned)((npa + 31) / 32);
+    if (nt > 65535) {
+      set_error("ao2mo: too many pairs for the expansion grid");
+      return PQ_ERR_ARG;
+    }
+    tc::expand_packed8_kernel<<<dim3(nt, nt), 256, 0, st>>>(eri_ao, npa, full.as<double>());
     PQ_CUDA_TRY(cudaGetLastError());
     pairs = full.as<double>();
   }
@@ -480,8 +512,8 @@ static pq_status ao2mo_tc_impl(const double *eri_ao, int layout, int64_t n, cons
   auto half = [&](const double *src64, const float *src32, int64_t ld_src, int64_t nslices, float *out) -> pq_status {
     for (int64_t b0 = 0; b0 < nslices; b0 += bt) {
       const int nb = (int)std::min(bt, nslices - b0);
-      tc::split_slices_kernel<TF32><<<152 * 32, 256, 0, st>>>(src64, src32, ld_src, (int)n, ld, b0, nb, sh.as<E>(),
-                                                              sl.as<E>());
+      tc::split_slices_kernel<TF32><<<(unsigned)nb, 256, 0, st>>>(src64, src32, ld_src, (int)n, ld, b0, sh.as<E>(),
+                                                                  sl.as<E>());
       PQ_CUDA_TRY(cudaGetLastError());
       // GEMM 1: U^T[b] (nm x n) = Ct (nm x n) . S[b]^T, K = n
       Operand S{sh.ptr, sl.ptr, (int64_t)nb * n, ld};
