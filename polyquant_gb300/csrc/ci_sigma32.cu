@@ -81,8 +81,10 @@ template <int NV, bool DIAG>
 __global__ void __launch_bounds__(256) rowside_kernel(RowSideArgs p) {
   extern __shared__ float jrow[];  // [e][k] = (pair_e | kk) for the row string's singles e
   using V = typename FVec<NV>::V;
-  const int64_t r = blockIdx.x / p.nblk;
-  const int64_t c = (blockIdx.x % p.nblk) * 256 + threadIdx.x;
+  // rows vary fastest: concurrently resident CTAs share one block of columns,
+  // so the partner rows they read stay in L2
+  const int64_t r = blockIdx.x % p.nrow;
+  const int64_t c = (blockIdx.x / p.nrow) * 256 + threadIdx.x;
   const int64_t e0 = p.s1_off[r];
   const int n1 = (int)(p.s1_off[r + 1] - e0);
   for (int t = threadIdx.x; t < n1 * p.n_orb; t += 256) {
@@ -186,20 +188,50 @@ __global__ void __launch_bounds__(128) ab_scatter_kernel(ABArgs p) {
   const float *w0 = W + (v0 ? i0 : 0) * ws;
   const float *w1 = W + (v1 ? i1 : 0) * ws;
   const float *xrow = p.X + Ja * p.nb * NV;
+  // per-warp staging of one beta string's partner vectors and coefficient codes
+  V *xs = reinterpret_cast<V *>(W + AB_MAXI * ws) + warp * AB_MAXI;
+  int *ps = reinterpret_cast<int *>(reinterpret_cast<V *>(W + AB_MAXI * ws) + 4 * AB_MAXI) + warp * AB_MAXI;
   const int64_t b_lo = (int64_t)ch * p.chunk, b_hi = (b_lo + p.chunk < p.nb) ? b_lo + p.chunk : p.nb;
-  for (int64_t Ib = b_lo + warp; Ib < b_hi; Ib += 4) {
+  // lane l fetches partners l and l + 32 of a beta string (coalesced table reads, one gather each)
+  auto fetch = [&](int64_t Ib, V &xa, V &xb, int &ia, int &ib, int &n) {
+    n = 0;
+    ia = ib = 0;
+    xa = xb = vzero<V>();
+    if (Ib >= b_hi) return;
+    const int64_t e0 = p.b_off[Ib];
+    n = (int)(p.b_off[Ib + 1] - e0);
+    if (lane < n) {
+      ia = __ldg(p.b_info + e0 + lane);
+      xa = FVec<NV>::ld(xrow + (int64_t)__ldg(p.b_J + e0 + lane) * NV);
+    }
+    if (lane + 32 < n) {
+      ib = __ldg(p.b_info + e0 + lane + 32);
+      xb = FVec<NV>::ld(xrow + (int64_t)__ldg(p.b_J + e0 + lane + 32) * NV);
+    }
+  };
+  V xa, xb;
+  int ia, ib, n;
+  int64_t Ib = b_lo + warp;
+  fetch(Ib, xa, xb, ia, ib, n);
+  for (; Ib < b_hi; Ib += 4) {
+    const int ncur = n;
+    xs[lane] = xa;
+    xs[lane + 32] = xb;
+    ps[lane] = ia;
+    ps[lane + 32] = ib;
+    __syncwarp();
+    fetch(Ib + 4, xa, xb, ia, ib, n);  // next string's loads overlap this string's arithmetic
     V acc0 = vzero<V>(), acc1 = vzero<V>();
-    const int64_t e0 = p.b_off[Ib], e1 = p.b_off[Ib + 1];
-#pragma unroll 8
-    for (int64_t e = e0; e < e1; e++) {
-      const int Jb = __ldg(p.b_J + e);
-      const int info = __ldg(p.b_info + e);
-      const V x = FVec<NV>::ld(xrow + (int64_t)Jb * NV);
+#pragma unroll 4
+    for (int j = 0; j < ncur; j++) {
+      const V x = xs[j];
+      const int info = ps[j];
       const int pb = info >> 1;
       const uint32_t neg = (uint32_t)(info & 1);
       vfma(acc0, fflip(w0[pb], neg), x);
       vfma(acc1, fflip(w1[pb], neg), x);
     }
+    __syncwarp();
     if (v0) atomicAdd(reinterpret_cast<V *>(p.Y + (row0 + Ib) * NV), acc0);
     if (v1) atomicAdd(reinterpret_cast<V *>(p.Y + (row1 + Ib) * NV), acc1);
   }
@@ -209,7 +241,7 @@ __global__ void __launch_bounds__(128) ab_scatter_kernel(ABArgs p) {
 bool sigma32_v2_applicable(const pq_ci_handle *h) {
   if (h->n_species != 1 || !h->full) return false;
   const int npair = h->npair[0];
-  if (h->tab[0][0].max1 > AB_MAXI) return false;
+  if (h->tab[0][0].max1 > AB_MAXI || h->tab[0][1].max1 > AB_MAXI) return false;
   const size_t wbytes = sizeof(float) * (size_t)AB_MAXI * (npair + 1);
   return wbytes <= 100 * 1024;
 }
@@ -282,7 +314,7 @@ static pq_status sigma32_v2_impl(pq_ci_handle *h, const float *X, float *Y, doub
   b.nchunks = (int)((nb + b.chunk - 1) / b.chunk);
   b.X = X;
   b.Y = Y;
-  const size_t smem = sizeof(float) * (size_t)AB_MAXI * (npair + 1);
+  const size_t smem = sizeof(float) * (size_t)AB_MAXI * (npair + 1) + (sizeof(float) * NV + sizeof(int)) * 4 * AB_MAXI;
   if (smem > 48 * 1024) PQ_CUDA_TRY(cudaFuncSetAttribute(ab_scatter_kernel<NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int64_t grid = na * b.nchunks;
   if (grid > 0x7fffffffLL) {
