@@ -219,6 +219,47 @@ def bench_ao2mo(n=256, L=1024, seed=0):
                          "note": "algorithmic flops; the split modes issue 3 MMAs per product"}}
 
 
+def bench_psh_like(seed=0):
+    """Electron-positron product space shaped like the PsH case: 1a1b electrons in 60 orbitals x 1 positron in 40
+    orbitals (144,000 determinants), seeded synthetic e-e, p-p and e-p integrals; sigma timings (FP64/FP32) and
+    3-root Davidson energies of the mixed path against FP64."""
+    import torch
+
+    from polyquant_gb300 import synthetic
+    from polyquant_gb300._lib import PQ_FP32, PQ_FP64
+    from polyquant_gb300.detset import POLYQUANT_DETSET
+
+    n_e, n_p = 60, 40
+    h_e, h_p, ee, pp, ep = synthetic.ep_integrals(n_e, n_p, seed=seed)
+    ds = POLYQUANT_DETSET([n_e, n_p], [1, 1], [1, 0], [[h_e, h_e], [h_p, h_p]],
+                          {(0, 0, 0, 0): ee, (1, 0, 1, 0): pp, (0, 0, 1, 0): ep}, [[1, 1, 2], [1, 0, 1]],
+                          restricted=[1, 1], charge=[-1.0, 1.0])
+    n = ds.N_dets
+    X = torch.randn(n, 3, device="cuda", dtype=torch.float64)
+    res = {"workload": f"e-p product space, electrons 1a1b in {n_e} orbitals x positron 1a in {n_p} orbitals, "
+                       f"{n:,} determinants, seed {seed}", "n_dets": n}
+    for name, prec in (("fp64", PQ_FP64), ("fp32", PQ_FP32)):
+        ds.sigma(X, precision=prec)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            ds.sigma(X, precision=prec)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 5
+        res[f"sigma_{name}_ms"] = ms
+        res[f"sigma_{name}_dets_per_s"] = n * 3 / (ms * 1e-3)
+    e64, i64 = ds.davidson(num_states=3, num_subspace_vec=6, convergence_E=1e-8, precision=PQ_FP64)
+    e32, i32 = ds.davidson(num_states=3, num_subspace_vec=6, convergence_E=1e-8, precision=PQ_FP32)
+    res["energies_fp64"] = e64.tolist()
+    res["davidson_fp64_s"] = i64["seconds"]
+    res["davidson_mixed_s"] = i32["seconds"]
+    res["max_abs_energy_error_mixed"] = float(np.abs(e32 - e64).max())
+    ds.close()
+    return res
+
+
 def time_to_solution(ds, roots=4, nsub=8, tol=1e-4):
     """Wall time of the FP64 and the mixed (FP32 sigma + FP64 refinement) Davidson to a residual that bounds the
     energy error well below 1 uEh, with each energy's error against a tightly converged FP64 solve."""
@@ -248,6 +289,7 @@ def main():
     ap.add_argument("--norb", type=int, default=N_ORB, help="smaller FCI case for profiling only")
     ap.add_argument("--nel", type=int, default=N_A, help="electrons per spin of the profiling case")
     ap.add_argument("--no-ao2mo", action="store_true")
+    ap.add_argument("--no-psh", action="store_true")
     ap.add_argument("--only-ao2mo", action="store_true", help="run only the AO->MO measurement (profiling case)")
     ap.add_argument("--tts", action="store_true", help="also measure time to 1 uEh (FP64 vs mixed Davidson)")
     args = ap.parse_args()
@@ -350,6 +392,9 @@ def main():
     tts = None
     if args.tts:
         tts = time_to_solution(ds, roots=ROOTS)
+    psh = None
+    if not args.no_psh and rank == 0:
+        psh = bench_psh_like()
     ao = None
     if not args.no_ao2mo and rank == 0:
         del X64, Y64, X32, Y32
@@ -376,6 +421,7 @@ def main():
                 "gpu_launches": args.steps,
                 "clocks": clk.summary(),
                 "ao2mo": ao,
+                "psh_like": psh,
                 "time_to_1uEh": tts,
                 "cpu_baseline": cb}
         print(json.dumps(line), flush=True)

@@ -167,32 +167,40 @@ constexpr int AB_MAXI = 64;  // alpha singles per string handled by one CTA (two
 
 template <int NV>
 __global__ void __launch_bounds__(128) ab_scatter_kernel(ABArgs p) {
-  extern __shared__ float W[];  // [i][pair_b], row stride npair + 1 (odd: conflict-free column reads)
+  // W2[pair_b][lane] = (coefficient of alpha single lane, of alpha single lane + 32):
+  // one 8-byte load per lane and partner, consecutive across the warp
+  extern __shared__ float2 W2[];
   using V = typename FVec<NV>::V;
   const int64_t Ja = blockIdx.x / p.nchunks;
   const int ch = (int)(blockIdx.x % p.nchunks);
   const int64_t a0 = p.a_off[Ja];
   const int n1 = (int)(p.a_off[Ja + 1] - a0);
-  const int ws = p.npair + 1;
-  for (int t = threadIdx.x; t < n1 * p.npair; t += 128) {
-    const int i = t / p.npair, q = t - i * p.npair;
-    const int info = p.a_info[a0 + i];
-    W[i * ws + q] = fflip(p.eab[(int64_t)(info >> 1) * p.npair + q], (uint32_t)(info & 1));
+  for (int t = threadIdx.x; t < 32 * p.npair; t += 128) {
+    const int q = t >> 5, l = t & 31;
+    float2 w = make_float2(0.f, 0.f);
+    if (l < n1) {
+      const int info = p.a_info[a0 + l];
+      w.x = fflip(p.eab[(int64_t)(info >> 1) * p.npair + q], (uint32_t)(info & 1));
+    }
+    if (l + 32 < n1) {
+      const int info = p.a_info[a0 + l + 32];
+      w.y = fflip(p.eab[(int64_t)(info >> 1) * p.npair + q], (uint32_t)(info & 1));
+    }
+    W2[q * 32 + l] = w;
   }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i0 = lane, i1 = lane + 32;
-  const bool v0 = i0 < n1, v1 = i1 < n1;
-  const int64_t row0 = v0 ? (int64_t)__ldg(p.a_J + a0 + i0) * p.nb : 0;
-  const int64_t row1 = v1 ? (int64_t)__ldg(p.a_J + a0 + i1) * p.nb : 0;
-  const float *w0 = W + (v0 ? i0 : 0) * ws;
-  const float *w1 = W + (v1 ? i1 : 0) * ws;
+  const bool v0 = lane < n1, v1 = lane + 32 < n1;
+  const int64_t row0 = v0 ? (int64_t)__ldg(p.a_J + a0 + lane) * p.nb : 0;
+  const int64_t row1 = v1 ? (int64_t)__ldg(p.a_J + a0 + lane + 32) * p.nb : 0;
+  const float2 *wl = W2 + lane;
   const float *xrow = p.X + Ja * p.nb * NV;
-  // per-warp staging of one beta string's partner vectors and coefficient codes
-  V *xs = reinterpret_cast<V *>(W + AB_MAXI * ws) + warp * AB_MAXI;
-  int *ps = reinterpret_cast<int *>(reinterpret_cast<V *>(W + AB_MAXI * ws) + 4 * AB_MAXI) + warp * AB_MAXI;
+  // per-warp staging of one beta string's signed partner vectors and pair codes
+  V *xs = reinterpret_cast<V *>(W2 + 32 * p.npair) + warp * AB_MAXI;
+  int *ps = reinterpret_cast<int *>(reinterpret_cast<V *>(W2 + 32 * p.npair) + 4 * AB_MAXI) + warp * AB_MAXI;
   const int64_t b_lo = (int64_t)ch * p.chunk, b_hi = (b_lo + p.chunk < p.nb) ? b_lo + p.chunk : p.nb;
-  // lane l fetches partners l and l + 32 of a beta string (coalesced table reads, one gather each)
+  // lane l fetches partners l and l + 32 of a beta string (coalesced table reads, one gather each);
+  // the partner's phase is applied to its vector here, once
   auto fetch = [&](int64_t Ib, V &xa, V &xb, int &ia, int &ib, int &n) {
     n = 0;
     ia = ib = 0;
@@ -201,12 +209,20 @@ __global__ void __launch_bounds__(128) ab_scatter_kernel(ABArgs p) {
     const int64_t e0 = p.b_off[Ib];
     n = (int)(p.b_off[Ib + 1] - e0);
     if (lane < n) {
-      ia = __ldg(p.b_info + e0 + lane);
+      const int info = __ldg(p.b_info + e0 + lane);
+      ia = info >> 1;
       xa = FVec<NV>::ld(xrow + (int64_t)__ldg(p.b_J + e0 + lane) * NV);
+      float *f = reinterpret_cast<float *>(&xa);
+#pragma unroll
+      for (int v = 0; v < NV; v++) f[v] = fflip(f[v], (uint32_t)(info & 1));
     }
     if (lane + 32 < n) {
-      ib = __ldg(p.b_info + e0 + lane + 32);
+      const int info = __ldg(p.b_info + e0 + lane + 32);
+      ib = info >> 1;
       xb = FVec<NV>::ld(xrow + (int64_t)__ldg(p.b_J + e0 + lane + 32) * NV);
+      float *f = reinterpret_cast<float *>(&xb);
+#pragma unroll
+      for (int v = 0; v < NV; v++) f[v] = fflip(f[v], (uint32_t)(info & 1));
     }
   };
   V xa, xb;
@@ -225,11 +241,9 @@ __global__ void __launch_bounds__(128) ab_scatter_kernel(ABArgs p) {
 #pragma unroll 4
     for (int j = 0; j < ncur; j++) {
       const V x = xs[j];
-      const int info = ps[j];
-      const int pb = info >> 1;
-      const uint32_t neg = (uint32_t)(info & 1);
-      vfma(acc0, fflip(w0[pb], neg), x);
-      vfma(acc1, fflip(w1[pb], neg), x);
+      const float2 w = wl[ps[j] * 32];
+      vfma(acc0, w.x, x);
+      vfma(acc1, w.y, x);
     }
     __syncwarp();
     if (v0) atomicAdd(reinterpret_cast<V *>(p.Y + (row0 + Ib) * NV), acc0);
@@ -242,7 +256,7 @@ bool sigma32_v2_applicable(const pq_ci_handle *h) {
   if (h->n_species != 1 || !h->full) return false;
   const int npair = h->npair[0];
   if (h->tab[0][0].max1 > AB_MAXI || h->tab[0][1].max1 > AB_MAXI) return false;
-  const size_t wbytes = sizeof(float) * (size_t)AB_MAXI * (npair + 1);
+  const size_t wbytes = sizeof(float) * (size_t)AB_MAXI * npair;
   return wbytes <= 100 * 1024;
 }
 
@@ -314,7 +328,7 @@ static pq_status sigma32_v2_impl(pq_ci_handle *h, const float *X, float *Y, doub
   b.nchunks = (int)((nb + b.chunk - 1) / b.chunk);
   b.X = X;
   b.Y = Y;
-  const size_t smem = sizeof(float) * (size_t)AB_MAXI * (npair + 1) + (sizeof(float) * NV + sizeof(int)) * 4 * AB_MAXI;
+  const size_t smem = sizeof(float2) * 32 * (size_t)npair + (sizeof(float) * NV + sizeof(int)) * 4 * AB_MAXI;
   if (smem > 48 * 1024) PQ_CUDA_TRY(cudaFuncSetAttribute(ab_scatter_kernel<NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int64_t grid = na * b.nchunks;
   if (grid > 0x7fffffffLL) {
