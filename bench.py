@@ -260,6 +260,50 @@ def bench_psh_like(seed=0):
     return res
 
 
+def bench_batch(n_problems=256, seed=0, roots=2, nsub=4, max_subspace=8, tol=1e-5):
+    """Batched uneven CI: n_problems full-CI problems drawn by synthetic.batch_specs (n_orb ~ U{8..14},
+    n_alpha, n_beta ~ U{2..n_orb//2}, 0-2 positrons in 6 orbitals, per-problem seeds), 2 roots each, solved
+    by the lockstep batched Davidson (one persistent sigma launch per iteration, CUDA graph, autotuned launch
+    shape) in FP64 and in mixed precision; problems/s of each and the per-problem energy error of the mixed
+    path against the FP64 energies."""
+    from polyquant_gb300 import synthetic
+    from polyquant_gb300._lib import PQ_FP32, PQ_FP64
+    from polyquant_gb300.batch import CIBatch
+
+    specs = synthetic.batch_specs(n_problems, seed)
+    sizes = np.array([synthetic.batch_spec_dets(s) for s in specs], dtype=np.int64)
+    t0 = time.time()
+    b = CIBatch([synthetic.batch_problem(s) for s in specs])
+    setup_s = time.time() - t0
+    assert list(sizes) == b.n_dets
+    res = {"workload": f"{n_problems} full-CI problems (seed {seed}): n_orb U{{8..14}}, n_alpha/n_beta "
+                       f"U{{2..n_orb/2}}, 0-2 positrons in 6 orbitals; {roots} roots each",
+           "n_problems": n_problems, "setup_seconds": setup_s,
+           "dets": {"total": int(sizes.sum()), "min": int(sizes.min()), "median": float(np.median(sizes)),
+                    "max": int(sizes.max()),
+                    "by_positrons": {str(k): int(sizes[[s["n_pos"] == k for s in specs]].sum()) for k in (0, 1, 2)},
+                    "count_over_1e6": int((sizes > 1_000_000).sum())},
+           "residual_tol": tol, "max_subspace": max_subspace}
+    out = {}
+    for name, prec in (("fp64", PQ_FP64), ("mixed", PQ_FP32)):
+        t0 = time.perf_counter()
+        e, info = b.davidson(num_states=roots, num_subspace_vec=nsub, convergence_E=tol, precision=prec,
+                             max_subspace=max_subspace)
+        dt = time.perf_counter() - t0
+        out[name] = e
+        res[name] = {"seconds": dt, "problems_per_s": n_problems / dt,
+                     "converged": int(sum(i["converged"] for i in info)),
+                     "iterations_max": int(max(i["iterations"] for i in info)),
+                     "sigma_calls_fp64": int(sum(i["sigma_calls_fp64"] for i in info)),
+                     "sigma_calls_fp32": int(sum(i["sigma_calls_fp32"] for i in info))}
+    err = np.abs(out["mixed"] - out["fp64"]).max(axis=1)
+    res["energy_error_mixed_vs_fp64"] = {"max": float(err.max()), "median": float(np.median(err)),
+                                         "count_over_1uEh": int((err > 1e-6).sum())}
+    res["tuning"] = b.tuning()
+    b.close()
+    return res
+
+
 def time_to_solution(ds, roots=4, nsub=8, tol=1e-4):
     """Wall time of the FP64 and the mixed (FP32 sigma + FP64 refinement) Davidson to a residual that bounds the
     energy error well below 1 uEh, with each energy's error against a tightly converged FP64 solve."""
@@ -292,6 +336,9 @@ def main():
     ap.add_argument("--no-psh", action="store_true")
     ap.add_argument("--only-ao2mo", action="store_true", help="run only the AO->MO measurement (profiling case)")
     ap.add_argument("--tts", action="store_true", help="also measure time to 1 uEh (FP64 vs mixed Davidson)")
+    ap.add_argument("--batch", action="store_true", help="also run the batched uneven-CI workload")
+    ap.add_argument("--only-batch", action="store_true", help="run only the batched uneven-CI workload")
+    ap.add_argument("--batch-problems", type=int, default=256)
     args = ap.parse_args()
     globals().update(N_ORB=args.norb, N_A=args.nel, N_B=args.nel)
 
@@ -306,6 +353,9 @@ def main():
     torch.cuda.set_device(local)
     if args.only_ao2mo:
         print(json.dumps(bench_ao2mo()), flush=True)
+        return
+    if args.only_batch:
+        print(json.dumps({"batched_ci": bench_batch(args.batch_problems)}), flush=True)
         return
     dist = None
     if world > 1:
@@ -402,6 +452,10 @@ def main():
         torch.cuda.empty_cache()
         ao = bench_ao2mo()
 
+    bt = None
+    if args.batch and rank == 0:
+        bt = bench_batch(args.batch_problems)
+
     cb = None
     if rank == 0 and not args.no_cpu:
         cb = cpu_baseline(budget_s=args.cpu_budget)
@@ -423,6 +477,7 @@ def main():
                 "ao2mo": ao,
                 "psh_like": psh,
                 "time_to_1uEh": tts,
+                "batched_ci": bt,
                 "cpu_baseline": cb}
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -21,6 +21,7 @@
  */
 #ifndef PQ_CI_H
 #define PQ_CI_H
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -146,12 +147,52 @@ typedef struct {
   int32_t converged;
   double max_residual;
   double seconds;
+  double sigma_seconds;      /* wall time of the sigma evaluations (layout conversion included) */
 } pq_davidson_report;
 
 /* energies: host, num_states doubles (shift included).  vecs: DEVICE buffer
  * n_dets x num_states column-major, or NULL. */
 pq_status pq_ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *energies, double *vecs,
                          pq_davidson_report *report);
+
+/* ---- batches of independent problems -------------------------------------
+ * Many small CI problems of uneven size solved together: one persistent sigma
+ * kernel per Davidson iteration covers every active problem (work units
+ * pulled from a device counter in descending cost order, FP64 and FP32
+ * problems in the same launch), and the per-iteration launch sequence is a
+ * CUDA graph replayed each iteration.  The reference runs one
+ * POLYQUANT_EPCI::run (src/ci/epci.cpp:575-686) per problem; these calls solve
+ * the same eigenproblems with the same sigma terms
+ * (src/ci/direct_singleparticle.cpp:238-372,
+ * src/ci/direct_mixedparticle.cpp:269-611).
+ *
+ * Every problem must be a full product of complete string spaces (full CI of
+ * species 0, optionally times full CI of species 1 with at most 40
+ * determinants); other problems are rejected with PQ_ERR_ARG.  stream may be
+ * NULL: the batch then owns a non-blocking stream and synchronises the device
+ * on entry to each call. */
+typedef struct pq_ci_batch pq_ci_batch;
+
+/* descs: n problem descriptions (integral pointers are read during the call only). */
+pq_status pq_ci_batch_create(const pq_ci_desc *descs, int32_t n, void *stream, pq_ci_batch **out);
+pq_status pq_ci_batch_destroy(pq_ci_batch *b);
+pq_status pq_ci_batch_num_dets(const pq_ci_batch *b, int32_t i, int64_t *n_dets);
+
+/* sigma = H C for every problem: C[i], S[i] DEVICE pointers to n_dets(i) x nvec
+ * column-major FP64 (ldc / lds may be NULL; else each entry must equal n_dets). */
+pq_status pq_ci_batch_sigma(pq_ci_batch *b, const double *const *C, const int64_t *ldc, int32_t nvec,
+                            double *const *S, const int64_t *lds, int32_t precision);
+
+/* Launch shape chosen by the autotuner on the first sigma or Davidson call
+ * (0, 0 before that). */
+pq_status pq_ci_batch_tuning(const pq_ci_batch *b, int32_t *warps_per_cta, int32_t *rows_per_unit);
+
+/* Block Davidson for every problem with the same parameters.  Problems are
+ * processed in groups whose Davidson buffers fit workspace_bytes (0: 80% of
+ * the free device memory).  energies: host, n x num_states; reports: host, n
+ * entries or NULL.  Returns PQ_NOT_CONVERGED if any problem did not converge. */
+pq_status pq_ci_batch_davidson(pq_ci_batch *b, const pq_davidson_params *p, size_t workspace_bytes,
+                               double *energies, pq_davidson_report *reports);
 
 #ifdef __cplusplus
 }

@@ -20,7 +20,8 @@ EXPORTS = [
     "pq_last_error", "pq_version", "pq_ci_create", "pq_ci_destroy", "pq_ci_num_dets", "pq_ci_strings",
     "pq_ci_det_unfold", "pq_ci_diag", "pq_ci_sigma", "pq_ci_sigma_host", "pq_ci_sigma_noalloc",
     "pq_ci_sigma_interleaved",
-    "pq_ci_davidson", "pq_ao2mo", "pq_mo1",
+    "pq_ci_davidson", "pq_ci_batch_create", "pq_ci_batch_destroy", "pq_ci_batch_num_dets", "pq_ci_batch_sigma",
+    "pq_ci_batch_tuning", "pq_ci_batch_davidson", "pq_ao2mo", "pq_mo1",
 ]
 
 
@@ -68,6 +69,7 @@ class PQDavidsonReport(ctypes.Structure):
         ("converged", ctypes.c_int32),
         ("max_residual", ctypes.c_double),
         ("seconds", ctypes.c_double),
+        ("sigma_seconds", ctypes.c_double),
     ]
 
 
@@ -104,6 +106,19 @@ def load(path: str = LIB_PATH):
     L.pq_ci_sigma_interleaved.argtypes = [P, P, P, I32, I32, D]
     L.pq_ci_davidson.restype = I32
     L.pq_ci_davidson.argtypes = [P, ctypes.POINTER(PQDavidsonParams), P, P, ctypes.POINTER(PQDavidsonReport)]
+    L.pq_ci_batch_create.restype = I32
+    L.pq_ci_batch_create.argtypes = [ctypes.POINTER(PQDesc), I32, P, ctypes.POINTER(P)]
+    L.pq_ci_batch_destroy.restype = I32
+    L.pq_ci_batch_destroy.argtypes = [P]
+    L.pq_ci_batch_num_dets.restype = I32
+    L.pq_ci_batch_num_dets.argtypes = [P, I32, ctypes.POINTER(I64)]
+    L.pq_ci_batch_sigma.restype = I32
+    L.pq_ci_batch_sigma.argtypes = [P, P, P, I32, P, P, I32]
+    L.pq_ci_batch_tuning.restype = I32
+    L.pq_ci_batch_tuning.argtypes = [P, ctypes.POINTER(I32), ctypes.POINTER(I32)]
+    L.pq_ci_batch_davidson.restype = I32
+    L.pq_ci_batch_davidson.argtypes = [P, ctypes.POINTER(PQDavidsonParams), ctypes.c_size_t, P,
+                                       ctypes.POINTER(PQDavidsonReport)]
     L.pq_ao2mo.restype = I32
     L.pq_ao2mo.argtypes = [P, I32, I64, I64, P, I64, I64, P, I64, I64, I32, P, P]
     L.pq_mo1.restype = I32

@@ -119,106 +119,22 @@ __global__ void unshift_kernel(const float *Y, int nvp, int nv, const double *V,
     for (int v = 0; v < nv; v++) W[i + v * ldw] = (double)Y[i * nvp + v] + s * V[i + v * ldv];
 }
 
-struct Davidson {
-  pq_ci_handle *h;
-  cublasHandle_t cb = nullptr;
-  int64_t n = 0;
-  DevBuf V, W, X, R, T, tmp, dth, didx, coef;
-  ~Davidson() {
-    if (cb) cublasDestroy(cb);
-  }
-  unsigned grid() const { return (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16); }
-
-  // sigma for nv columns of src (ld n) into dst (ld n); FP32 path applies shift s
-  pq_status sigma(const double *src, double *dst, int nv, int precision, double s, pq_davidson_report *rep) {
-    if (precision == PQ_FP64) {
-      for (int v0 = 0; v0 < nv; v0 += 4) {
-        int c = std::min(4, nv - v0), nvp = c == 1 ? 1 : (c == 2 ? 2 : 4);
-        PQ_TRY(h->x_il.ensure(sizeof(double) * nvp * (size_t)(n + 1)));
-        PQ_TRY(h->y_il.ensure(sizeof(double) * nvp * (size_t)(n + 1)));
-        PQ_TRY(ci_to_il(h, src, n, v0, c, nvp, PQ_FP64, h->x_il.ptr));
-        PQ_TRY(ci_sigma_il(h, h->x_il.ptr, h->y_il.ptr, nvp, PQ_FP64, 0.0));
-        PQ_TRY(ci_from_il(h, h->y_il.ptr, v0, c, nvp, PQ_FP64, dst, n));
-      }
-      rep->sigma_calls_fp64++;
-    } else {
-      for (int v0 = 0; v0 < nv; v0 += 4) {
-        int c = std::min(4, nv - v0), nvp = c == 1 ? 1 : (c == 2 ? 2 : 4);
-        PQ_TRY(h->x_il.ensure(sizeof(float) * nvp * (size_t)(n + 1)));
-        PQ_TRY(h->y_il.ensure(sizeof(float) * nvp * (size_t)(n + 1)));
-        PQ_TRY(ci_to_il(h, src, n, v0, c, nvp, PQ_FP32, h->x_il.ptr));
-        PQ_TRY(ci_sigma_il(h, h->x_il.ptr, h->y_il.ptr, nvp, PQ_FP32, s));
-        unshift_kernel<<<grid(), 256, 0, h->stream>>>((const float *)h->y_il.ptr, nvp, c, src + (size_t)v0 * n, n, s, n,
-                                                       dst + (size_t)v0 * n, n);
-        PQ_CUDA_TRY(cudaGetLastError());
-      }
-      rep->sigma_calls_fp32++;
-    }
-    return PQ_OK;
-  }
-
-  // G = V[:, 0:m]^T W[:, 0:m] on the host (symmetrised)
-  pq_status rayleigh(int m, std::vector<double> &G) {
-    PQ_TRY(tmp.ensure(sizeof(double) * (size_t)m * m));
-    const double one = 1.0, zero = 0.0;
-    PQ_CUBLAS_TRY(cublasDgemm(cb, CUBLAS_OP_T, CUBLAS_OP_N, m, m, (int)n, &one, V.as<double>(), (int)n, W.as<double>(),
-                              (int)n, &zero, tmp.as<double>(), m));
-    G.resize((size_t)m * m);
-    PQ_CUDA_TRY(cudaMemcpyAsync(G.data(), tmp.ptr, sizeof(double) * m * m, cudaMemcpyDeviceToHost, h->stream));
-    PQ_CUDA_TRY(cudaStreamSynchronize(h->stream));
-    for (int i = 0; i < m; i++)
-      for (int j = i + 1; j < m; j++) {
-        double s = 0.5 * (G[i + (size_t)j * m] + G[j + (size_t)i * m]);
-        G[i + (size_t)j * m] = G[j + (size_t)i * m] = s;
-      }
-    return PQ_OK;
-  }
-
-  // Orthonormalise columns T[:, 0:k] against V[:, 0:m] and each other (two
-  // classical Gram-Schmidt passes); accepted columns are appended to V.
-  pq_status orthonormalize_append(int m, int k, int *added) {
-    const double one = 1.0, mone = -1.0, zero = 0.0;
-    PQ_TRY(coef.ensure(sizeof(double) * (size_t)(m + k) * 2));
-    int mm = m;
-    for (int j = 0; j < k; j++) {
-      double *t = T.as<double>() + (size_t)j * n;
-      double nrm0 = 0.0;
-      PQ_CUBLAS_TRY(cublasDnrm2(cb, (int)n, t, 1, &nrm0));
-      if (!(nrm0 > 0.0) || !std::isfinite(nrm0)) continue;
-      for (int pass = 0; pass < 2; pass++) {
-        PQ_CUBLAS_TRY(cublasDgemv(cb, CUBLAS_OP_T, (int)n, mm, &one, V.as<double>(), (int)n, t, 1, &zero,
-                                  coef.as<double>(), 1));
-        PQ_CUBLAS_TRY(cublasDgemv(cb, CUBLAS_OP_N, (int)n, mm, &mone, V.as<double>(), (int)n, coef.as<double>(), 1,
-                                  &one, t, 1));
-      }
-      double nrm = 0.0;
-      PQ_CUBLAS_TRY(cublasDnrm2(cb, (int)n, t, 1, &nrm));
-      if (!(nrm > 1e-8 * nrm0) || nrm < 1e-300) continue;
-      double inv = 1.0 / nrm;
-      PQ_CUBLAS_TRY(cublasDscal(cb, (int)n, &inv, t, 1));
-      PQ_CUDA_TRY(cudaMemcpyAsync(V.as<double>() + (size_t)mm * n, t, sizeof(double) * n, cudaMemcpyDeviceToDevice,
-                                  h->stream));
-      mm++;
-    }
-    *added = mm - m;
-    return PQ_OK;
-  }
-};
-
-pq_status ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *energies, double *vecs,
-                      pq_davidson_report *rep_out) {
-  auto t_start = std::chrono::steady_clock::now();
-  pq_davidson_report rep{};
-  Davidson D;
-  D.h = h;
-  D.n = h->n_dets;
-  const int64_t n = D.n;
-  int k = p->num_states;
+// One Davidson solve as a step-wise state machine: init() and advance() stop
+// whenever sigma vectors are needed (a SigmaRequest), so one driver can serve a
+// single problem and a lockstep batch of problems with one sigma launch per
+// iteration.
+pq_status DavidsonRun::init(pq_ci_handle *hh, const pq_davidson_params &pp, ::cublasContext *shared_cb) {
+  t_start = std::chrono::steady_clock::now();
+  h = hh;
+  p = pp;
+  n = h->n_dets;
+  k = p.num_states;
+  st = h->stream;
   if (k < 1 || n < 1) {
     set_error("davidson: num_states=%d, n_dets=%lld", k, (long long)n);
     return PQ_ERR_ARG;
   }
-  if (p->precision != PQ_FP64 && p->precision != PQ_FP32) {
+  if (p.precision != PQ_FP64 && p.precision != PQ_FP32) {
     set_error("davidson: precision must be PQ_FP64 or PQ_FP32");
     return PQ_ERR_ARG;
   }
@@ -226,8 +142,8 @@ pq_status ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *ener
     set_error("davidson: n_dets beyond the 32-bit cuBLAS dimension limit");
     return PQ_ERR_ARG;
   }
-  int m0 = std::max(p->num_subspace_vec, k);
-  int mmax = p->max_subspace > 0 ? p->max_subspace : std::max(2 * p->num_subspace_vec, 10 * k);
+  m0 = std::max(p.num_subspace_vec, k);
+  mmax = p.max_subspace > 0 ? p.max_subspace : std::max(2 * p.num_subspace_vec, 10 * k);
   mmax = std::max(mmax, m0 + k);
   if ((int64_t)m0 > n) m0 = (int)n;
   if ((int64_t)mmax > n) mmax = (int)n;
@@ -235,21 +151,28 @@ pq_status ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *ener
     set_error("davidson: num_states %d exceeds the space dimension %lld", k, (long long)n);
     return PQ_ERR_ARG;
   }
-  const int iter_max = p->iteration_max > 0 ? p->iteration_max : 500;
-  const double tol = p->convergence_E > 0 ? p->convergence_E : 1e-6;
-  cudaStream_t st = h->stream;
-  if (cublasCreate(&D.cb) != CUBLAS_STATUS_SUCCESS) {
-    set_error("cublasCreate failed");
-    return PQ_ERR_CUDA;
+  iter_max = p.iteration_max > 0 ? p.iteration_max : 500;
+  tol = p.convergence_E > 0 ? p.convergence_E : 1e-6;
+  switch_tol = std::max(tol, 1e-5);
+  phase32 = p.precision == PQ_FP32;
+  if (shared_cb) {
+    cb = shared_cb;
+  } else {
+    if (cublasCreate(&cb) != CUBLAS_STATUS_SUCCESS) {
+      set_error("cublasCreate failed");
+      return PQ_ERR_CUDA;
+    }
+    own_cb = true;
+    PQ_CUBLAS_TRY(cublasSetStream(cb, st));
   }
-  PQ_CUBLAS_TRY(cublasSetStream(D.cb, st));
-  PQ_TRY(D.V.alloc(sizeof(double) * (size_t)n * mmax));
-  PQ_TRY(D.W.alloc(sizeof(double) * (size_t)n * mmax));
-  PQ_TRY(D.X.alloc(sizeof(double) * (size_t)n * k));
-  PQ_TRY(D.R.alloc(sizeof(double) * (size_t)n * k));
-  PQ_TRY(D.T.alloc(sizeof(double) * (size_t)n * std::max(k, m0)));
-  PQ_TRY(D.dth.alloc(sizeof(double) * std::max(k, 8)));
-
+  PQ_TRY(V.alloc(sizeof(double) * (size_t)n * mmax));
+  PQ_TRY(W.alloc(sizeof(double) * (size_t)n * mmax));
+  PQ_TRY(X.alloc(sizeof(double) * (size_t)n * k));
+  PQ_TRY(R.alloc(sizeof(double) * (size_t)n * k));
+  PQ_TRY(T.alloc(sizeof(double) * (size_t)n * std::max(k, m0)));
+  PQ_TRY(dth.alloc(sizeof(double) * std::max(k, 8)));
+  theta.assign(k, 0.0);
+  rnorm.assign(k, 0.0);
   // initial subspace: unit vectors at the m0 smallest diagonal elements
   std::vector<double> diag(n);
   PQ_CUDA_TRY(cudaMemcpyAsync(diag.data(), h->d_diag.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
@@ -259,87 +182,128 @@ pq_status ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *ener
   auto cmp = [&](int64_t a, int64_t b) { return diag[a] < diag[b] || (diag[a] == diag[b] && a < b); };
   std::partial_sort(idx.begin(), idx.begin() + m0, idx.end(), cmp);
   idx.resize(m0);
-  double shift = diag[idx[0]];
-  PQ_TRY(upload(D.didx, idx, st));
-  unit_vectors_kernel<<<D.grid(), 256, 0, st>>>(D.V.as<double>(), n, D.didx.as<int64_t>(), m0);
+  shift = diag[idx[0]];
+  PQ_TRY(upload(didx, idx, st));
+  unit_vectors_kernel<<<grid(), 256, 0, st>>>(V.as<double>(), n, didx.as<int64_t>(), m0);
   PQ_CUDA_TRY(cudaGetLastError());
-  // unit vectors are exact in FP32: their sigma is computed in FP64 to start
-  PQ_TRY(D.sigma(D.V.as<double>(), D.W.as<double>(), m0, PQ_FP64, 0.0, &rep));
-  int m = m0;
-  bool exact = true;  // every column of W is an FP64 sigma
-  std::vector<double> G, w, Z;
-  std::vector<double> theta(k), rnorm(k);
-  const double one = 1.0, mone = -1.0, zero = 0.0;
-  int it = 0;
-  bool force_refine = false;
-  bool phase32 = p->precision == PQ_FP32;
-  bool just_refined = false;
-  double last_refined = 1e300;
-  const double switch_tol = std::max(tol, 1e-5);
-  pq_status result = PQ_NOT_CONVERGED;
-  for (it = 1; it <= iter_max; it++) {
-    PQ_TRY(D.rayleigh(m, G));
+  if (h->n_species == 1) {
+    // sigma of a unit vector is a column of H: exact FP64 from its connections
+    PQ_TRY(ci_unit_columns(h, idx, W.as<double>()));
+    pending = false;
+    stage = AFTER_INIT;
+  } else {
+    request(V.as<double>(), W.as<double>(), m0, PQ_FP64, 0.0, AFTER_INIT);
+  }
+  return PQ_OK;
+}
+
+void DavidsonRun::request(const double *src, double *dst, int cnt, int prec, double s, Stage next) {
+  req = SigmaRequest{src, dst, cnt, prec, s};
+  pending = true;
+  stage = next;
+  if (prec == PQ_FP64)
+    rep.sigma_calls_fp64++;
+  else
+    rep.sigma_calls_fp32++;
+}
+
+pq_status DavidsonRun::advance() {
+  const double one = 1.0, zero = 0.0;
+  pending = false;
+  switch (stage) {
+    case AFTER_INIT:
+      m = m0;
+      exact = true;
+      break;
+    case AFTER_REFINE:
+      exact = true;
+      just_refined = true;
+      m = r_restart;
+      break;
+    case AFTER_NEW:
+      if (req.precision == PQ_FP32) exact = false;
+      m += req.cnt;
+      break;
+    default:
+      break;
+  }
+  std::vector<double> G, w;
+  while (true) {
+    it++;
+    if (it > iter_max) {
+      it = iter_max;
+      return finish_state(PQ_NOT_CONVERGED);
+    }
+    PQ_TRY(rayleigh(m, G));
     jacobi_eigh(m, G, w, Z);
     for (int i = 0; i < k; i++) theta[i] = w[i];
-    PQ_TRY(D.tmp.ensure(sizeof(double) * (size_t)m * k));
+    PQ_TRY(tmp.ensure(sizeof(double) * (size_t)m * k));
     std::vector<double> Yk(Z.begin(), Z.begin() + (size_t)m * k);
-    PQ_CUDA_TRY(cudaMemcpyAsync(D.tmp.ptr, Yk.data(), sizeof(double) * m * k, cudaMemcpyHostToDevice, st));
+    PQ_CUDA_TRY(cudaMemcpyAsync(tmp.ptr, Yk.data(), sizeof(double) * m * k, cudaMemcpyHostToDevice, st));
     // X = V Y, R = W Y - X theta
-    PQ_CUBLAS_TRY(cublasDgemm(D.cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, k, m, &one, D.V.as<double>(), (int)n,
-                              D.tmp.as<double>(), m, &zero, D.X.as<double>(), (int)n));
-    PQ_CUBLAS_TRY(cublasDgemm(D.cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, k, m, &one, D.W.as<double>(), (int)n,
-                              D.tmp.as<double>(), m, &zero, D.R.as<double>(), (int)n));
+    PQ_CUBLAS_TRY(cublasDgemm(cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, k, m, &one, V.as<double>(), (int)n,
+                              tmp.as<double>(), m, &zero, X.as<double>(), (int)n));
+    PQ_CUBLAS_TRY(cublasDgemm(cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, k, m, &one, W.as<double>(), (int)n,
+                              tmp.as<double>(), m, &zero, R.as<double>(), (int)n));
     double maxr = 0.0;
     for (int i = 0; i < k; i++) {
       double mt = -theta[i];
-      PQ_CUBLAS_TRY(cublasDaxpy(D.cb, (int)n, &mt, D.X.as<double>() + (size_t)i * n, 1, D.R.as<double>() + (size_t)i * n, 1));
-      PQ_CUBLAS_TRY(cublasDnrm2(D.cb, (int)n, D.R.as<double>() + (size_t)i * n, 1, &rnorm[i]));
+      PQ_CUBLAS_TRY(cublasDaxpy(cb, (int)n, &mt, X.as<double>() + (size_t)i * n, 1, R.as<double>() + (size_t)i * n, 1));
+      PQ_CUBLAS_TRY(cublasDnrm2(cb, (int)n, R.as<double>() + (size_t)i * n, 1, &rnorm[i]));
       maxr = std::max(maxr, rnorm[i]);
     }
-    if (p->verbose) {
+    if (p.verbose) {
       printf("davidson it %3d  m %3d  %s", it, m, exact ? "fp64" : "mixd");
-      for (int i = 0; i < k; i++) printf("  E%d % .12f r %.2e", i, theta[i] + p->energy_shift, rnorm[i]);
+      for (int i = 0; i < k; i++) printf("  E%d % .12f r %.2e", i, theta[i] + p.energy_shift, rnorm[i]);
       printf("\n");
     }
     rep.max_residual = maxr;
-    if (maxr < tol && exact) {
-      result = PQ_OK;
-      break;
-    }
-    // Mixed precision: FP32 sigma for new directions while the exact
-    // (refined) residual keeps improving; once it stalls near the FP32 noise
-    // floor, or gets close to the target, switch to FP64 directions.
+    if (maxr < tol && exact) return finish_state(PQ_OK);
+    // Mixed precision: FP32 sigma for new directions.  The FP32 phase drives
+    // the (inexact) residual to a fraction of the target so that a single
+    // FP64 refinement usually finishes the solve; it refines early when the
+    // inexact residual stops improving (the FP32 noise floor), and switches to
+    // FP64 directions only when two refinements in a row made no progress.
     if (phase32 && exact && just_refined) {
-      if (maxr < 4.0 * switch_tol || maxr > 0.5 * last_refined) phase32 = false;
+      if (maxr > 0.5 * last_refined) phase32 = false;
       last_refined = maxr;
+      best32 = 1e300;
+      stall32 = 0;
+    }
+    if (phase32 && !exact) {
+      if (maxr < 0.9 * best32) {
+        best32 = maxr;
+        stall32 = 0;
+      } else {
+        stall32++;
+      }
     }
     just_refined = false;
-    bool refine = !exact && (!phase32 || maxr < switch_tol || force_refine);
-    bool need_restart = (m + k > mmax) || refine;
+    const bool refine = !exact && (!phase32 || maxr < 0.3 * switch_tol || stall32 >= 3 || force_refine);
+    const bool need_restart = (m + k > mmax) || refine;
     force_refine = false;
     if (need_restart) {
       // mixed precision restarts keep only the Ritz vectors: each refinement
       // is then one FP64 sigma call for the k roots
-      int r = (refine || p->precision == PQ_FP32) ? k : std::min(m0, m);
+      int r = (refine || p.precision == PQ_FP32) ? k : std::min(m0, m);
       r = std::max(r, k);
       // V[:, 0:r] = V Z[:, 0:r]; W likewise (via the temporary T)
-      PQ_TRY(D.tmp.ensure(sizeof(double) * (size_t)m * r));
+      PQ_TRY(tmp.ensure(sizeof(double) * (size_t)m * r));
       std::vector<double> Zr(Z.begin(), Z.begin() + (size_t)m * r);
-      PQ_CUDA_TRY(cudaMemcpyAsync(D.tmp.ptr, Zr.data(), sizeof(double) * m * r, cudaMemcpyHostToDevice, st));
-      PQ_TRY(D.T.ensure(sizeof(double) * (size_t)n * r));
-      PQ_CUBLAS_TRY(cublasDgemm(D.cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, r, m, &one, D.V.as<double>(), (int)n,
-                                D.tmp.as<double>(), m, &zero, D.T.as<double>(), (int)n));
-      PQ_CUDA_TRY(cudaMemcpyAsync(D.V.ptr, D.T.ptr, sizeof(double) * n * r, cudaMemcpyDeviceToDevice, st));
+      PQ_CUDA_TRY(cudaMemcpyAsync(tmp.ptr, Zr.data(), sizeof(double) * m * r, cudaMemcpyHostToDevice, st));
+      PQ_TRY(T.ensure(sizeof(double) * (size_t)n * r));
+      PQ_CUBLAS_TRY(cublasDgemm(cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, r, m, &one, V.as<double>(), (int)n,
+                                tmp.as<double>(), m, &zero, T.as<double>(), (int)n));
+      PQ_CUDA_TRY(cudaMemcpyAsync(V.ptr, T.ptr, sizeof(double) * n * r, cudaMemcpyDeviceToDevice, st));
       if (!exact) {
         // FP64 residual refinement: exact sigma of the restart vectors
-        PQ_TRY(D.sigma(D.V.as<double>(), D.W.as<double>(), r, PQ_FP64, 0.0, &rep));
-        exact = true;
-        just_refined = true;
-      } else {
-        PQ_CUBLAS_TRY(cublasDgemm(D.cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, r, m, &one, D.W.as<double>(), (int)n,
-                                  D.tmp.as<double>(), m, &zero, D.T.as<double>(), (int)n));
-        PQ_CUDA_TRY(cudaMemcpyAsync(D.W.ptr, D.T.ptr, sizeof(double) * n * r, cudaMemcpyDeviceToDevice, st));
+        r_restart = r;
+        request(V.as<double>(), W.as<double>(), r, PQ_FP64, 0.0, AFTER_REFINE);
+        return PQ_OK;
       }
+      PQ_CUBLAS_TRY(cublasDgemm(cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, r, m, &one, W.as<double>(), (int)n,
+                                tmp.as<double>(), m, &zero, T.as<double>(), (int)n));
+      PQ_CUDA_TRY(cudaMemcpyAsync(W.ptr, T.ptr, sizeof(double) * n * r, cudaMemcpyDeviceToDevice, st));
       m = r;
       continue;
     }
@@ -348,42 +312,135 @@ pq_status ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *ener
     std::vector<double> th_u;
     for (int i = 0; i < k; i++) {
       if (rnorm[i] < tol) continue;
-      PQ_CUDA_TRY(cudaMemcpyAsync(D.T.as<double>() + (size_t)nt * n, D.R.as<double>() + (size_t)i * n,
-                                  sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+      PQ_CUDA_TRY(cudaMemcpyAsync(T.as<double>() + (size_t)nt * n, R.as<double>() + (size_t)i * n, sizeof(double) * n,
+                                  cudaMemcpyDeviceToDevice, st));
       th_u.push_back(theta[i]);
       nt++;
     }
-    PQ_CUDA_TRY(cudaMemcpyAsync(D.dth.ptr, th_u.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, st));
-    precondition_kernel<<<D.grid(), 256, 0, st>>>(D.T.as<double>(), h->d_diag.as<double>(), D.dth.as<double>(), n, nt,
-                                                  D.T.as<double>());
+    PQ_CUDA_TRY(cudaMemcpyAsync(dth.ptr, th_u.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, st));
+    precondition_kernel<<<grid(), 256, 0, st>>>(T.as<double>(), h->d_diag.as<double>(), dth.as<double>(), n, nt,
+                                                T.as<double>());
     PQ_CUDA_TRY(cudaGetLastError());
     int added = 0;
-    PQ_TRY(D.orthonormalize_append(m, nt, &added));
+    PQ_TRY(orthonormalize_append(m, nt, &added));
     if (added == 0) {
       // no new direction: the subspace is invariant to working precision
-      if (exact) {
-        result = PQ_OK;
-        break;
-      }
+      if (exact) return finish_state(PQ_OK);
       force_refine = true;
       continue;
     }
     shift = theta[0];
     const int prec = phase32 ? PQ_FP32 : PQ_FP64;
-    PQ_TRY(D.sigma(D.V.as<double>() + (size_t)m * n, D.W.as<double>() + (size_t)m * n, added, prec, shift, &rep));
-    if (prec == PQ_FP32) exact = false;
-    m += added;
+    request(V.as<double>() + (size_t)m * n, W.as<double>() + (size_t)m * n, added, prec, shift, AFTER_NEW);
+    return PQ_OK;
   }
-  rep.iterations = std::min(it, iter_max);
-  rep.converged = result == PQ_OK;
-  for (int i = 0; i < k; i++) energies[i] = theta[i] + p->energy_shift;
-  if (vecs) PQ_CUDA_TRY(cudaMemcpyAsync(vecs, D.X.ptr, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, st));
+}
+
+pq_status DavidsonRun::finish_state(pq_status r) {
+  done = true;
+  result = r;
+  rep.iterations = it;
+  rep.converged = r == PQ_OK;
+  return PQ_OK;
+}
+
+pq_status DavidsonRun::outputs(double *energies, double *vecs) {
+  for (int i = 0; i < k; i++) energies[i] = theta[i] + p.energy_shift;
+  if (vecs) PQ_CUDA_TRY(cudaMemcpyAsync(vecs, X.ptr, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, st));
   PQ_CUDA_TRY(cudaStreamSynchronize(st));
   rep.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
-  if (rep_out) *rep_out = rep;
-  if (result != PQ_OK) set_error("davidson: not converged after %d iterations (max residual %.3e)", iter_max, rep.max_residual);
-  (void)mone;
-  return result;
+  return PQ_OK;
+}
+
+DavidsonRun::~DavidsonRun() {
+  if (cb && own_cb) cublasDestroy(cb);
+}
+
+// G = V[:, 0:m]^T W[:, 0:m] on the host (symmetrised)
+pq_status DavidsonRun::rayleigh(int mm, std::vector<double> &G) {
+  PQ_TRY(tmp.ensure(sizeof(double) * (size_t)mm * mm));
+  const double one = 1.0, zero = 0.0;
+  PQ_CUBLAS_TRY(cublasDgemm(cb, CUBLAS_OP_T, CUBLAS_OP_N, mm, mm, (int)n, &one, V.as<double>(), (int)n, W.as<double>(),
+                            (int)n, &zero, tmp.as<double>(), mm));
+  G.resize((size_t)mm * mm);
+  PQ_CUDA_TRY(cudaMemcpyAsync(G.data(), tmp.ptr, sizeof(double) * mm * mm, cudaMemcpyDeviceToHost, st));
+  PQ_CUDA_TRY(cudaStreamSynchronize(st));
+  for (int i = 0; i < mm; i++)
+    for (int j = i + 1; j < mm; j++) {
+      double s = 0.5 * (G[i + (size_t)j * mm] + G[j + (size_t)i * mm]);
+      G[i + (size_t)j * mm] = G[j + (size_t)i * mm] = s;
+    }
+  return PQ_OK;
+}
+
+// Orthonormalise columns T[:, 0:kk] against V[:, 0:mm] and each other (two
+// classical Gram-Schmidt passes); accepted columns are appended to V.
+pq_status DavidsonRun::orthonormalize_append(int mm0, int kk, int *added) {
+  const double one = 1.0, mone = -1.0, zero = 0.0;
+  PQ_TRY(coef.ensure(sizeof(double) * (size_t)(mm0 + kk) * 2));
+  int mm = mm0;
+  for (int j = 0; j < kk; j++) {
+    double *t = T.as<double>() + (size_t)j * n;
+    double nrm0 = 0.0;
+    PQ_CUBLAS_TRY(cublasDnrm2(cb, (int)n, t, 1, &nrm0));
+    if (!(nrm0 > 0.0) || !std::isfinite(nrm0)) continue;
+    for (int pass = 0; pass < 2; pass++) {
+      PQ_CUBLAS_TRY(cublasDgemv(cb, CUBLAS_OP_T, (int)n, mm, &one, V.as<double>(), (int)n, t, 1, &zero, coef.as<double>(), 1));
+      PQ_CUBLAS_TRY(cublasDgemv(cb, CUBLAS_OP_N, (int)n, mm, &mone, V.as<double>(), (int)n, coef.as<double>(), 1, &one, t, 1));
+    }
+    double nrm = 0.0;
+    PQ_CUBLAS_TRY(cublasDnrm2(cb, (int)n, t, 1, &nrm));
+    if (!(nrm > 1e-8 * nrm0) || nrm < 1e-300) continue;
+    double inv = 1.0 / nrm;
+    PQ_CUBLAS_TRY(cublasDscal(cb, (int)n, &inv, t, 1));
+    PQ_CUDA_TRY(cudaMemcpyAsync(V.as<double>() + (size_t)mm * n, t, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    mm++;
+  }
+  *added = mm - mm0;
+  return PQ_OK;
+}
+
+// sigma of a request for one problem: column-major FP64 in and out; the FP32
+// path applies (H - shift) and adds shift * src back in FP64
+pq_status sigma_request_single(pq_ci_handle *h, const SigmaRequest &r) {
+  const int64_t n = h->n_dets;
+  const unsigned g = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16);
+  for (int v0 = 0; v0 < r.cnt; v0 += 4) {
+    const int c = std::min(4, r.cnt - v0), nvp = c == 1 ? 1 : (c == 2 ? 2 : 4);
+    const size_t esz = r.precision == PQ_FP64 ? sizeof(double) : sizeof(float);
+    PQ_TRY(h->x_il.ensure(esz * nvp * (size_t)(n + 1)));
+    PQ_TRY(h->y_il.ensure(esz * nvp * (size_t)(n + 1)));
+    PQ_TRY(ci_to_il(h, r.src, n, v0, c, nvp, r.precision, h->x_il.ptr));
+    PQ_TRY(ci_sigma_il(h, h->x_il.ptr, h->y_il.ptr, nvp, r.precision, r.precision == PQ_FP64 ? 0.0 : r.shift));
+    if (r.precision == PQ_FP64) {
+      PQ_TRY(ci_from_il(h, h->y_il.ptr, v0, c, nvp, PQ_FP64, r.dst, n));
+    } else {
+      unshift_kernel<<<g, 256, 0, h->stream>>>((const float *)h->y_il.ptr, nvp, c, r.src + (size_t)v0 * n, n, r.shift, n,
+                                               r.dst + (size_t)v0 * n, n);
+      PQ_CUDA_TRY(cudaGetLastError());
+    }
+  }
+  return PQ_OK;
+}
+
+pq_status ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *energies, double *vecs,
+                      pq_davidson_report *rep_out) {
+  DavidsonRun D;
+  PQ_TRY(D.init(h, *p));
+  while (!D.done) {
+    if (D.pending) {
+      const auto t0 = std::chrono::steady_clock::now();
+      PQ_TRY(sigma_request_single(h, D.req));
+      PQ_CUDA_TRY(cudaStreamSynchronize(h->stream));
+      D.rep.sigma_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    PQ_TRY(D.advance());
+  }
+  PQ_TRY(D.outputs(energies, vecs));
+  if (rep_out) *rep_out = D.rep;
+  if (D.result != PQ_OK)
+    set_error("davidson: not converged after %d iterations (max residual %.3e)", D.iter_max, D.rep.max_residual);
+  return D.result;
 }
 
 }  // namespace pq

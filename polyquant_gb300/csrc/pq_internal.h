@@ -3,11 +3,14 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <chrono>
 #include <string>
 #include <vector>
 
 #include "pq_ci.h"
 #include "pq_ints.h"
+
+struct cublasContext;  // cuBLAS handle type (cublasHandle_t)
 
 namespace pq {
 
@@ -124,6 +127,8 @@ pq_status ci_unfold2(const pq_ci_handle *h, int32_t *out);
 // allow_scratch = false keeps sigma on kernels that need no work memory beyond X and Y
 pq_status ci_sigma_il(pq_ci_handle *h, const void *X, void *Y, int nvec, int precision, double shift,
                       bool allow_scratch = true);
+// exact FP64 columns H[:, dets[c]] into column-major W (one species)
+pq_status ci_unit_columns(pq_ci_handle *h, const std::vector<int64_t> &dets, double *W);
 // ci_sigma32.cu
 bool sigma32_v2_applicable(const pq_ci_handle *h);
 pq_status ci_sigma32_v2(pq_ci_handle *h, const void *X, void *Y, int nvp, double shift);
@@ -132,4 +137,53 @@ pq_status ci_from_il(pq_ci_handle *h, const void *Y, int v0, int nv, int nvp, in
 // ci_davidson.cu
 pq_status ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *energies, double *vecs,
                       pq_davidson_report *rep);
+
+// A pending sigma evaluation of a Davidson run: dst = H src for cnt columns
+// (column-major, leading dimension n_dets); FP32 requests use (H - shift) in
+// FP32 and add shift * src back in FP64.
+struct SigmaRequest {
+  const double *src;
+  double *dst;
+  int cnt;
+  int precision;
+  double shift;
+};
+pq_status sigma_request_single(pq_ci_handle *h, const SigmaRequest &r);
+
+class DavidsonRun {
+ public:
+  enum Stage { NONE, AFTER_INIT, AFTER_REFINE, AFTER_NEW };
+  // shared_cb: a cuBLAS handle bound to h->stream that the run borrows (else it creates its own)
+  pq_status init(pq_ci_handle *h, const pq_davidson_params &p, ::cublasContext *shared_cb = nullptr);
+  pq_status advance();  // after the pending request was evaluated
+  pq_status outputs(double *energies, double *vecs);
+  ~DavidsonRun();
+  bool pending = false, done = false;
+  SigmaRequest req{};
+  pq_status result = PQ_NOT_CONVERGED;
+  pq_davidson_report rep{};
+  std::vector<double> theta, rnorm;
+  int iter_max = 500;
+  pq_ci_handle *h = nullptr;
+  int64_t n = 0;
+
+ private:
+  void request(const double *src, double *dst, int cnt, int prec, double s, Stage next);
+  pq_status finish_state(pq_status r);
+  pq_status rayleigh(int m, std::vector<double> &G);
+  pq_status orthonormalize_append(int m, int k, int *added);
+  unsigned grid() const { return (unsigned)((n + 255) / 256 < 152 * 16 ? (n + 255) / 256 : 152 * 16); }
+  pq_davidson_params p{};
+  cudaStream_t st = nullptr;
+  ::cublasContext *cb = nullptr;
+  bool own_cb = false;
+  DevBuf V, W, X, R, T, tmp, dth, didx, coef;
+  std::vector<double> Z;
+  int k = 0, m0 = 0, mmax = 0, m = 0, it = 0, r_restart = 0;
+  double tol = 1e-6, switch_tol = 1e-5, shift = 0.0, last_refined = 1e300, best32 = 1e300;
+  int stall32 = 0;
+  bool exact = true, phase32 = false, just_refined = false, force_refine = false;
+  Stage stage = NONE;
+  std::chrono::steady_clock::time_point t_start;
+};
 }  // namespace pq

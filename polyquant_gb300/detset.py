@@ -29,6 +29,48 @@ def _torch():
     return torch
 
 
+def make_desc(n_orb: Sequence[int], n_alpha: Sequence[int], n_beta: Sequence[int], h1, eri: Dict,
+              excitation_level: Sequence[Sequence[int]], restricted: Sequence[int] = None,
+              charge: Sequence[float] = None, max_collective_excitation_level: int = INT_MAX):
+    """pq_ci_desc for one problem plus the Fortran-ordered integral arrays it points to (keep them alive
+    until the create call returns)."""
+    ns = len(n_orb)
+    restricted = list(restricted) if restricted is not None else [1] * ns
+    charge = list(charge) if charge is not None else [-1.0] * ns
+    d = _lib.PQDesc()
+    d.n_species = ns
+    keep = []
+    for s in range(ns):
+        d.n_orb[s] = int(n_orb[s])
+        d.n_alpha[s] = int(n_alpha[s])
+        d.n_beta[s] = int(n_beta[s])
+        d.restricted[s] = int(restricted[s])
+        d.charge[s] = float(charge[s])
+        for t in range(3):
+            d.ex_level[s][t] = int(excitation_level[s][t])
+        nb = 1 if restricted[s] else 2
+        for sp in range(2):
+            m = np.asfortranarray(np.asarray(h1[s][sp % nb] if len(h1[s]) > sp % nb else h1[s][0],
+                                             dtype=np.float64))
+            keep.append(m)
+            d.h1[s][sp] = m.ctypes.data
+    d.max_collective = int(max_collective_excitation_level)
+    for a in range(ns):
+        for sa in range(2):
+            for b in range(a, ns):
+                for sb in range(2):
+                    key = (a, sa % (1 if restricted[a] else 2), b, sb % (1 if restricted[b] else 2))
+                    m = eri.get(key)
+                    if m is None and a == b and (a, key[3], a, key[1]) in eri:
+                        m = np.asarray(eri[(a, key[3], a, key[1])]).T
+                    if m is None:
+                        continue
+                    m = np.asfortranarray(np.asarray(m, dtype=np.float64))
+                    keep.append(m)
+                    d.eri[a][sa][b][sb] = m.ctypes.data
+    return d, keep
+
+
 class POLYQUANT_DETSET:
     """Determinant space + Hamiltonian operator built on the GPU.
 
@@ -44,39 +86,8 @@ class POLYQUANT_DETSET:
                  charge: Sequence[float] = None, max_collective_excitation_level: int = INT_MAX, stream=None):
         L = _lib.load()
         ns = len(n_orb)
-        restricted = list(restricted) if restricted is not None else [1] * ns
-        charge = list(charge) if charge is not None else [-1.0] * ns
-        d = _lib.PQDesc()
-        d.n_species = ns
-        self._keep = []
-        for s in range(ns):
-            d.n_orb[s] = int(n_orb[s])
-            d.n_alpha[s] = int(n_alpha[s])
-            d.n_beta[s] = int(n_beta[s])
-            d.restricted[s] = int(restricted[s])
-            d.charge[s] = float(charge[s])
-            for t in range(3):
-                d.ex_level[s][t] = int(excitation_level[s][t])
-            nb = 1 if restricted[s] else 2
-            for sp in range(2):
-                m = np.asfortranarray(np.asarray(h1[s][sp % nb] if len(h1[s]) > sp % nb else h1[s][0],
-                                                 dtype=np.float64))
-                self._keep.append(m)
-                d.h1[s][sp] = m.ctypes.data
-        d.max_collective = int(max_collective_excitation_level)
-        for a in range(ns):
-            for sa in range(2):
-                for b in range(a, ns):
-                    for sb in range(2):
-                        key = (a, sa % (1 if restricted[a] else 2), b, sb % (1 if restricted[b] else 2))
-                        m = eri.get(key)
-                        if m is None and a == b and (a, key[3], a, key[1]) in eri:
-                            m = np.asarray(eri[(a, key[3], a, key[1])]).T
-                        if m is None:
-                            continue
-                        m = np.asfortranarray(np.asarray(m, dtype=np.float64))
-                        self._keep.append(m)
-                        d.eri[a][sa][b][sb] = m.ctypes.data
+        d, self._keep = make_desc(n_orb, n_alpha, n_beta, h1, eri, excitation_level, restricted, charge,
+                                  max_collective_excitation_level)
         self._desc = d
         self._stream = stream
         h = ctypes.c_void_p()
@@ -189,7 +200,7 @@ class POLYQUANT_DETSET:
         check(st, "pq_ci_davidson")
         info = dict(iterations=rep.iterations, converged=bool(rep.converged), max_residual=rep.max_residual,
                     sigma_calls_fp64=rep.sigma_calls_fp64, sigma_calls_fp32=rep.sigma_calls_fp32,
-                    seconds=rep.seconds)
+                    seconds=rep.seconds, sigma_seconds=rep.sigma_seconds)
         if return_vectors:
             return e, vecs.t(), info
         return e, info

@@ -101,3 +101,46 @@ def ao_eri_packed8(n: int, seed: int = 0, L: int = 1024) -> np.ndarray:
     """8-fold packed AO ERIs (host numpy; intended for small n)."""
     Bp = ao_eri_pairs(n, seed, L)
     return packed8_from_pairs(Bp.T @ Bp)
+
+
+def batch_specs(n_problems: int = 256, seed: int = 0, n_pos_orb: int = 6):
+    """Shapes of the batched uneven-CI workload: n_orb ~ U{8..14}, n_alpha, n_beta ~ U{2..n_orb//2},
+    0-2 positrons (1 = one alpha positron, 2 = one alpha + one beta) in n_pos_orb orbitals; each
+    problem's integrals use seed * 100003 + index."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(n_problems):
+        n = int(rng.integers(8, 15))
+        a = int(rng.integers(2, n // 2 + 1))
+        b = int(rng.integers(2, n // 2 + 1))
+        npos = int(rng.integers(0, 3))
+        specs.append(dict(n_orb=n, n_alpha=a, n_beta=b, n_pos=npos, n_pos_orb=n_pos_orb, seed=seed * 100003 + i))
+    return specs
+
+
+def _comb(n, k):
+    from math import comb
+
+    return comb(n, k)
+
+
+def batch_spec_dets(s) -> int:
+    p = {0: 1, 1: s["n_pos_orb"], 2: s["n_pos_orb"] ** 2}[s["n_pos"]]
+    return _comb(s["n_orb"], s["n_alpha"]) * _comb(s["n_orb"], s["n_beta"]) * p
+
+
+def batch_problem(s) -> dict:
+    """Full-CI problem of one spec as keyword arguments of POLYQUANT_DETSET / CIBatch."""
+    n, a, b = s["n_orb"], s["n_alpha"], s["n_beta"]
+    ex_e = [min(a, n - a), min(b, n - b), min(a, n - a) + min(b, n - b)]
+    if s["n_pos"] == 0:
+        h, eri = fci_integrals(n, s["seed"])
+        return dict(n_orb=[n], n_alpha=[a], n_beta=[b], h1=[[h]], eri={(0, 0, 0, 0): eri}, excitation_level=[ex_e],
+                    restricted=[1], charge=[-1.0])
+    m = s["n_pos_orb"]
+    pa, pb = (1, 0) if s["n_pos"] == 1 else (1, 1)
+    h_e, h_p, ee, pp, ep = ep_integrals(n, m, s["seed"])
+    ex_p = [min(pa, m - pa), min(pb, m - pb), min(pa, m - pa) + min(pb, m - pb)]
+    return dict(n_orb=[n, m], n_alpha=[a, pa], n_beta=[b, pb], h1=[[h_e], [h_p]],
+                eri={(0, 0, 0, 0): ee, (1, 0, 1, 0): pp, (0, 0, 1, 0): ep}, excitation_level=[ex_e, ex_p],
+                restricted=[1, 1], charge=[-1.0, 1.0])

@@ -47,3 +47,9 @@ def synthetic_ep(n_e, ne_a, ne_b, n_p, np_a, np_b, seed=0, ex_e=None, ex_p=None,
     return O.CIProblem([n_e, n_p], [ne_a, np_a], [ne_b, np_b], [[h_e, h_e], [h_p, h_p]],
                        {(0, 0, 0, 0): ee, (1, 0, 1, 0): pp, (0, 0, 1, 0): ep},
                        [ex_e, ex_p], restricted=[1, 1], charge=[-1.0, 1.0], max_collective=max_coll)
+
+
+def batch_dict(p):
+    """CIProblem -> keyword dict of CIBatch / POLYQUANT_DETSET."""
+    return dict(n_orb=p.n_orb, n_alpha=p.n_alpha, n_beta=p.n_beta, h1=p.h1, eri=p.eri, excitation_level=p.ex_level,
+                restricted=p.restricted, charge=p.charge, max_collective_excitation_level=p.max_collective)
