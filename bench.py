@@ -295,7 +295,8 @@ def bench_batch(n_problems=256, seed=0, roots=2, nsub=4, max_subspace=8, tol=1e-
                      "converged": int(sum(i["converged"] for i in info)),
                      "iterations_max": int(max(i["iterations"] for i in info)),
                      "sigma_calls_fp64": int(sum(i["sigma_calls_fp64"] for i in info)),
-                     "sigma_calls_fp32": int(sum(i["sigma_calls_fp32"] for i in info))}
+                     "sigma_calls_fp32": int(sum(i["sigma_calls_fp32"] for i in info)),
+                     "sigma_seconds": float(max(i["sigma_seconds"] for i in info))}
     err = np.abs(out["mixed"] - out["fp64"]).max(axis=1)
     res["energy_error_mixed_vs_fp64"] = {"max": float(err.max()), "median": float(np.median(err)),
                                          "count_over_1uEh": int((err > 1e-6).sum())}
@@ -314,7 +315,8 @@ def time_to_solution(ds, roots=4, nsub=8, tol=1e-4):
                          "residual": 1e-7}}
     for name, prec in (("fp64", PQ_FP64), ("mixed", PQ_FP32)):
         e, info = ds.davidson(num_states=roots, num_subspace_vec=nsub, convergence_E=tol, precision=prec)
-        res[name] = {"seconds": info["seconds"], "iterations": info["iterations"], "converged": info["converged"],
+        res[name] = {"seconds": info["seconds"], "sigma_seconds": info["sigma_seconds"],
+                     "iterations": info["iterations"], "converged": info["converged"],
                      "sigma_calls_fp64": info["sigma_calls_fp64"], "sigma_calls_fp32": info["sigma_calls_fp32"],
                      "max_abs_energy_error": float(np.abs(e - e_ref).max()), "residual": tol}
     res["speedup_mixed_vs_fp64"] = res["fp64"]["seconds"] / res["mixed"]["seconds"]

@@ -89,13 +89,13 @@ __device__ __forceinline__ int pairdiag(int k) { return k * (k + 3) / 2; }  // i
 
 // One work unit: rows (ia, b0 .. b0+nrows-1) of one problem, one warp.
 // Lanes form R = 32 / G groups of G lanes; a group owns one row and lane gl of
-// the group owns the row's columns gl, gl + G, ... (< L).  Matrix elements
-// are computed G at a time (one per lane) and broadcast with shuffles.
-template <typename T>
-__device__ void do_unit(const Prob &p, const Call &cl, const Unit &U, T *stg, int lane) {
+// the group owns the row's columns gl + j * G (j < J, < L).  Matrix elements
+// are computed G at a time (one per lane) and broadcast with shuffles; rows
+// are addressed by 32-bit row indices and one 64-bit base per connection.
+template <typename T, int J>
+__device__ void do_rows(const Prob &p, const Call &cl, const Unit &U, T *stg, int lane, int G) {
   const ProbT<T> &q = pt<T>(p);
   const int P = p.P, lw = cl.lw, L = P << lw;
-  const int G = L >= 32 ? 32 : (L <= 1 ? 1 : 1 << (32 - __clz(L - 1)));
   const int R = 32 / G, g = lane / G, gl = lane - g * G;
   const T *__restrict__ X = (const T *)cl.X;
   T *__restrict__ Y = (T *)cl.Y;
@@ -106,11 +106,12 @@ __device__ void do_unit(const Prob &p, const Call &cl, const Unit &U, T *stg, in
   const int a2n = (int)(p.a2_off[ia + 1] - a2b);
   const uint64_t amask = p.astr[ia];
   const T cf = (T)p.cf;
+  const int rowa = ia * nb;
   T *srow = stg + g * G;  // staging of one row (L <= G when R > 1)
   for (int r0 = 0; r0 < U.nrows; r0 += R) {
     const bool rok = r0 + g < U.nrows;
     const int ib = rok ? U.b0 + r0 + g : 0;
-    const int64_t Ie = (int64_t)ia * nb + ib;
+    const int Ie = rowa + ib;
     const int64_t b1b = p.b1_off[ib];
     const int b1n = rok ? (int)(p.b1_off[ib + 1] - b1b) : 0;
     const int64_t b2b = p.b2_off[ib];
@@ -118,23 +119,28 @@ __device__ void do_unit(const Prob &p, const Call &cl, const Unit &U, T *stg, in
     const uint64_t bmask = p.bstr[ib];
     const int b1max = __reduce_max_sync(0xffffffffu, b1n);
     const int b2max = __reduce_max_sync(0xffffffffu, b2n);
-    T acc[JMAX];
+    T acc[J];
+    {
+      const T *xr = X + (int64_t)Ie * L;
+      const double *dg = p.diag + (int64_t)Ie * P;
 #pragma unroll
-    for (int j = 0; j < JMAX; j++) {
-      const int c = gl + j * G;
-      acc[j] = T(0);
-      if (rok && c < L) {
-        const T x = X[Ie * L + c];
-        acc[j] = (T)(p.diag[Ie * P + (c >> lw)] - cl.shift) * x;
-        if (P > 1) srow[c] = x;
+      for (int j = 0; j < J; j++) {
+        const int c = gl + j * G;
+        acc[j] = T(0);
+        if (rok && c < L) {
+          const T x = xr[c];
+          acc[j] = (T)(dg[c >> lw] - cl.shift) * x;
+          if (P > 1) srow[c] = x;
+        }
       }
     }
     // positron terms inside the row: positron singles and doubles, and the
     // electron-diagonal x positron-single cross term
     if (P > 1) {
       __syncwarp();
+      const T *dea = q.dea + (int64_t)ia * 2 * npp, *deb = q.deb + (int64_t)ib * 2 * npp;
 #pragma unroll
-      for (int j = 0; j < JMAX; j++) {
+      for (int j = 0; j < J; j++) {
         const int c = gl + j * G;
         if (!rok || c >= L) continue;
         const int Jp = c >> lw, v = c & ((1 << lw) - 1);
@@ -142,7 +148,7 @@ __device__ void do_unit(const Prob &p, const Call &cl, const Unit &U, T *stg, in
         for (int e = p.ps_off[Jp]; e < p.ps_off[Jp + 1]; e++) {
           const int code = p.ps_code[e];
           const int Ip = code & 255, y = (code >> 8) & 1, prs = code >> 10;
-          const T de = q.dea[((int64_t)ia * 2 + y) * npp + prs] + q.deb[((int64_t)ib * 2 + y) * npp + prs];
+          const T de = dea[y * npp + prs] + deb[y * npp + prs];
           const T t = q.ps_h[e] + ((code >> 9) & 1 ? -cf : cf) * de;
           s += t * srow[(Ip << lw) + v];
         }
@@ -158,7 +164,7 @@ __device__ void do_unit(const Prob &p, const Call &cl, const Unit &U, T *stg, in
       const int nmax = x == 0 ? a1n : b1max;
       for (int t0 = 0; t0 < nmax; t0 += G) {
         const int t = t0 + gl;
-        int64_t Je = -1;
+        int Jr = -1;
         T val = T(0);
         int ph = 0, ng = 0;
         if (x == 0 && t < a1n && rok) {
@@ -167,9 +173,10 @@ __device__ void do_unit(const Prob &p, const Call &cl, const Unit &U, T *stg, in
           ph = info >> 1;
           ng = info & 1;
           T f = q.a1F[e];
-          for (uint64_t m = bmask; m; m &= m - 1) f += q.eab[(int64_t)ph * npe + pairdiag(__ffsll((long long)m) - 1)];
+          const T *er = q.eab + (int64_t)ph * npe;
+          for (uint64_t m = bmask; m; m &= m - 1) f += er[pairdiag(__ffsll((long long)m) - 1)];
           val = ng ? -f : f;
-          Je = (int64_t)p.a1_J[e] * nb + ib;
+          Jr = p.a1_J[e] * nb + ib;
         } else if (x == 1 && t < b1n) {
           const int64_t e = b1b + t;
           const int info = p.b1_info[e];
@@ -178,40 +185,48 @@ __device__ void do_unit(const Prob &p, const Call &cl, const Unit &U, T *stg, in
           T f = q.b1F[e];
           for (uint64_t m = amask; m; m &= m - 1) f += q.eab[(int64_t)pairdiag(__ffsll((long long)m) - 1) * npe + ph];
           val = ng ? -f : f;
-          Je = (int64_t)ia * nb + p.b1_J[e];
+          Jr = rowa + p.b1_J[e];
         }
         const int cnt = min(G, nmax - t0);
-        for (int i = 0; i < cnt; i++) {
-          const int64_t Ji = __shfl_sync(0xffffffffu, Je, i, G);
-          const T vi = __shfl_sync(0xffffffffu, val, i, G);
-          if (P == 1) {
+        if (P == 1) {
+#pragma unroll 4
+          for (int i = 0; i < cnt; i++) {
+            const int Ji = __shfl_sync(0xffffffffu, Jr, i, G);
+            const T vi = __shfl_sync(0xffffffffu, val, i, G);
             if (Ji >= 0) {
+              const T *xr = X + (int64_t)Ji * L;
 #pragma unroll
-              for (int j = 0; j < JMAX; j++) {
+              for (int j = 0; j < J; j++) {
                 const int c = gl + j * G;
-                if (c < L) acc[j] += vi * X[Ji * L + c];
+                if (c < L) acc[j] += vi * xr[c];
               }
             }
-          } else {
+          }
+        } else {
+          for (int i = 0; i < cnt; i++) {
+            const int Ji = __shfl_sync(0xffffffffu, Jr, i, G);
+            const T vi = __shfl_sync(0xffffffffu, val, i, G);
             const int phi = __shfl_sync(0xffffffffu, ph, i, G);
             const int ngi = __shfl_sync(0xffffffffu, ng, i, G);
-            T xv[JMAX];
+            const T *xr = X + (int64_t)(Ji >= 0 ? Ji : 0) * L;
+            T xv[J];
 #pragma unroll
-            for (int j = 0; j < JMAX; j++) {
+            for (int j = 0; j < J; j++) {
               const int c = gl + j * G;
-              xv[j] = (Ji >= 0 && c < L) ? X[Ji * L + c] : T(0);
+              xv[j] = (Ji >= 0 && c < L) ? xr[c] : T(0);
               if (c < L) srow[c] = xv[j];
             }
             __syncwarp();
             if (Ji >= 0) {
               const T sc = ngi ? -cf : cf;
+              const T *dpt = q.dpt + ((int64_t)x * npe + phi) * P;
+              const T *epx0 = q.ep[x][0] + (int64_t)phi * npp, *epx1 = q.ep[x][1] + (int64_t)phi * npp;
 #pragma unroll
-              for (int j = 0; j < JMAX; j++) {
+              for (int j = 0; j < J; j++) {
                 const int c = gl + j * G;
                 if (c >= L) continue;
                 const int Jp = c >> lw, v = c & ((1 << lw) - 1);
-                T s = (vi + sc * q.dpt[((int64_t)x * npe + phi) * P + Jp]) * xv[j];
-                const T *epx0 = q.ep[x][0] + (int64_t)phi * npp, *epx1 = q.ep[x][1] + (int64_t)phi * npp;
+                T s = (vi + sc * dpt[Jp]) * xv[j];
                 for (int e = p.ps_off[Jp]; e < p.ps_off[Jp + 1]; e++) {
                   const int code = p.ps_code[e];
                   const int Ip = code & 255, prs = code >> 10;
@@ -232,24 +247,26 @@ __device__ void do_unit(const Prob &p, const Call &cl, const Unit &U, T *stg, in
       const int nmax = x == 0 ? a2n : b2max;
       for (int t0 = 0; t0 < nmax; t0 += G) {
         const int t = t0 + gl;
-        int64_t Je = -1;
+        int Jr = -1;
         T val = T(0);
         if (x == 0 && t < a2n && rok) {
           val = q.a2D[a2b + t];
-          Je = (int64_t)p.a2_J[a2b + t] * nb + ib;
+          Jr = p.a2_J[a2b + t] * nb + ib;
         } else if (x == 1 && t < b2n) {
           val = q.b2D[b2b + t];
-          Je = (int64_t)ia * nb + p.b2_J[b2b + t];
+          Jr = rowa + p.b2_J[b2b + t];
         }
         const int cnt = min(G, nmax - t0);
+#pragma unroll 4
         for (int i = 0; i < cnt; i++) {
-          const int64_t Ji = __shfl_sync(0xffffffffu, Je, i, G);
+          const int Ji = __shfl_sync(0xffffffffu, Jr, i, G);
           const T vi = __shfl_sync(0xffffffffu, val, i, G);
           if (Ji >= 0) {
+            const T *xr = X + (int64_t)Ji * L;
 #pragma unroll
-            for (int j = 0; j < JMAX; j++) {
+            for (int j = 0; j < J; j++) {
               const int c = gl + j * G;
-              if (c < L) acc[j] += vi * X[Ji * L + c];
+              if (c < L) acc[j] += vi * xr[c];
             }
           }
         }
@@ -260,38 +277,56 @@ __device__ void do_unit(const Prob &p, const Call &cl, const Unit &U, T *stg, in
     for (int s = 0; s < a1n; s++) {
       const int64_t ea = a1b + s;
       const int infa = p.a1_info[ea];
-      const int64_t rowa = (int64_t)p.a1_J[ea] * nb;
+      const int rowj = p.a1_J[ea] * nb;
       const T *erow = q.eab + (int64_t)(infa >> 1) * npe;
       for (int t0 = 0; t0 < b1max; t0 += G) {
         const int t = t0 + gl;
-        int64_t Je = -1;
+        int Jr = -1;
         T val = T(0);
         if (t < b1n) {
           const int infb = p.b1_info[b1b + t];
           const T v = erow[infb >> 1];
           val = ((infa ^ infb) & 1) ? -v : v;
-          Je = rowa + p.b1_J[b1b + t];
+          Jr = rowj + p.b1_J[b1b + t];
         }
         const int cnt = min(G, b1max - t0);
+#pragma unroll 4
         for (int i = 0; i < cnt; i++) {
-          const int64_t Ji = __shfl_sync(0xffffffffu, Je, i, G);
+          const int Ji = __shfl_sync(0xffffffffu, Jr, i, G);
           const T vi = __shfl_sync(0xffffffffu, val, i, G);
           if (Ji >= 0) {
+            const T *xr = X + (int64_t)Ji * L;
 #pragma unroll
-            for (int j = 0; j < JMAX; j++) {
+            for (int j = 0; j < J; j++) {
               const int c = gl + j * G;
-              if (c < L) acc[j] += vi * X[Ji * L + c];
+              if (c < L) acc[j] += vi * xr[c];
             }
           }
         }
       }
     }
+    {
+      T *yr = Y + (int64_t)Ie * L;
 #pragma unroll
-    for (int j = 0; j < JMAX; j++) {
-      const int c = gl + j * G;
-      if (rok && c < L) Y[Ie * L + c] = acc[j];
+      for (int j = 0; j < J; j++) {
+        const int c = gl + j * G;
+        if (rok && c < L) yr[c] = acc[j];
+      }
     }
     __syncwarp();
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void do_unit(const Prob &p, const Call &cl, const Unit &U, T *stg, int lane) {
+  const int L = p.P << cl.lw;
+  const int G = L >= 32 ? 32 : (L <= 1 ? 1 : 1 << (32 - __clz(L - 1)));
+  switch ((L + G - 1) / G) {
+    case 1: do_rows<T, 1>(p, cl, U, stg, lane, G); break;
+    case 2: do_rows<T, 2>(p, cl, U, stg, lane, G); break;
+    case 3: do_rows<T, 3>(p, cl, U, stg, lane, G); break;
+    case 4: do_rows<T, 4>(p, cl, U, stg, lane, G); break;
+    default: do_rows<T, JMAX>(p, cl, U, stg, lane, G); break;
   }
 }
 

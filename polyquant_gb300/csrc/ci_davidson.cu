@@ -88,6 +88,18 @@ static void jacobi_eigh(int n, std::vector<double> A, std::vector<double> &w, st
   Z.swap(Zs);
 }
 
+// C[:, j] = op(A) B[:, j] for j < q, one DGEMV per column.  A is the tall
+// n x m block of V or W (n up to ~1e9 rows, m <= a few dozen columns): DGEMV
+// streams it at the FP64 FMA rate, while DGEMM on these shapes runs an order
+// of magnitude slower.
+static pq_status tall_skinny(cublasHandle_t cb, cublasOperation_t op, int64_t n, int m, const double *A,
+                             const double *B, int64_t ldb, int q, double *C, int64_t ldc) {
+  const double one = 1.0, zero = 0.0;
+  for (int j = 0; j < q; j++)
+    PQ_CUBLAS_TRY(cublasDgemv(cb, op, (int)n, m, &one, A, (int)n, B + (size_t)j * ldb, 1, &zero, C + (size_t)j * ldc, 1));
+  return PQ_OK;
+}
+
 __global__ void unit_vectors_kernel(double *V, int64_t n, const int64_t *idx, int m) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -219,6 +231,7 @@ pq_status DavidsonRun::advance() {
       exact = true;
       just_refined = true;
       m = r_restart;
+      g_valid = 0;
       break;
     case AFTER_NEW:
       if (req.precision == PQ_FP32) exact = false;
@@ -241,10 +254,8 @@ pq_status DavidsonRun::advance() {
     std::vector<double> Yk(Z.begin(), Z.begin() + (size_t)m * k);
     PQ_CUDA_TRY(cudaMemcpyAsync(tmp.ptr, Yk.data(), sizeof(double) * m * k, cudaMemcpyHostToDevice, st));
     // X = V Y, R = W Y - X theta
-    PQ_CUBLAS_TRY(cublasDgemm(cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, k, m, &one, V.as<double>(), (int)n,
-                              tmp.as<double>(), m, &zero, X.as<double>(), (int)n));
-    PQ_CUBLAS_TRY(cublasDgemm(cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, k, m, &one, W.as<double>(), (int)n,
-                              tmp.as<double>(), m, &zero, R.as<double>(), (int)n));
+    PQ_TRY(tall_skinny(cb, CUBLAS_OP_N, n, m, V.as<double>(), tmp.as<double>(), m, k, X.as<double>(), n));
+    PQ_TRY(tall_skinny(cb, CUBLAS_OP_N, n, m, W.as<double>(), tmp.as<double>(), m, k, R.as<double>(), n));
     double maxr = 0.0;
     for (int i = 0; i < k; i++) {
       double mt = -theta[i];
@@ -253,7 +264,8 @@ pq_status DavidsonRun::advance() {
       maxr = std::max(maxr, rnorm[i]);
     }
     if (p.verbose) {
-      printf("davidson it %3d  m %3d  %s", it, m, exact ? "fp64" : "mixd");
+      printf("davidson it %3d  m %3d  %s  t %8.3f s  sigma %8.3f s", it, m, exact ? "fp64" : "mixd",
+             std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count(), rep.sigma_seconds);
       for (int i = 0; i < k; i++) printf("  E%d % .12f r %.2e", i, theta[i] + p.energy_shift, rnorm[i]);
       printf("\n");
     }
@@ -283,27 +295,31 @@ pq_status DavidsonRun::advance() {
     const bool need_restart = (m + k > mmax) || refine;
     force_refine = false;
     if (need_restart) {
-      // mixed precision restarts keep only the Ritz vectors: each refinement
-      // is then one FP64 sigma call for the k roots
-      int r = (refine || p.precision == PQ_FP32) ? k : std::min(m0, m);
+      // a refinement restarts from the k Ritz vectors (one FP64 sigma call
+      // for the k roots); a restart for subspace size keeps min(m0, m)
+      // vectors and rotates W with V, inexact FP32 columns included (the
+      // next refinement replaces them)
+      int r = refine ? k : std::min(m0, m);
       r = std::max(r, k);
       // V[:, 0:r] = V Z[:, 0:r]; W likewise (via the temporary T)
       PQ_TRY(tmp.ensure(sizeof(double) * (size_t)m * r));
       std::vector<double> Zr(Z.begin(), Z.begin() + (size_t)m * r);
       PQ_CUDA_TRY(cudaMemcpyAsync(tmp.ptr, Zr.data(), sizeof(double) * m * r, cudaMemcpyHostToDevice, st));
       PQ_TRY(T.ensure(sizeof(double) * (size_t)n * r));
-      PQ_CUBLAS_TRY(cublasDgemm(cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, r, m, &one, V.as<double>(), (int)n,
-                                tmp.as<double>(), m, &zero, T.as<double>(), (int)n));
+      PQ_TRY(tall_skinny(cb, CUBLAS_OP_N, n, m, V.as<double>(), tmp.as<double>(), m, r, T.as<double>(), n));
       PQ_CUDA_TRY(cudaMemcpyAsync(V.ptr, T.ptr, sizeof(double) * n * r, cudaMemcpyDeviceToDevice, st));
-      if (!exact) {
+      if (refine) {
         // FP64 residual refinement: exact sigma of the restart vectors
         r_restart = r;
         request(V.as<double>(), W.as<double>(), r, PQ_FP64, 0.0, AFTER_REFINE);
         return PQ_OK;
       }
-      PQ_CUBLAS_TRY(cublasDgemm(cb, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, r, m, &one, W.as<double>(), (int)n,
-                                tmp.as<double>(), m, &zero, T.as<double>(), (int)n));
+      PQ_TRY(tall_skinny(cb, CUBLAS_OP_N, n, m, W.as<double>(), tmp.as<double>(), m, r, T.as<double>(), n));
       PQ_CUDA_TRY(cudaMemcpyAsync(W.ptr, T.ptr, sizeof(double) * n * r, cudaMemcpyDeviceToDevice, st));
+      // the rotated Rayleigh matrix Z_r^T G Z_r is diag(w) (Z diagonalises G)
+      for (int j = 0; j < r; j++)
+        for (int i = 0; i < r; i++) Gk[i + (size_t)j * mmax] = i == j ? w[i] : 0.0;
+      g_valid = r;
       m = r;
       continue;
     }
@@ -356,20 +372,32 @@ DavidsonRun::~DavidsonRun() {
   if (cb && own_cb) cublasDestroy(cb);
 }
 
-// G = V[:, 0:m]^T W[:, 0:m] on the host (symmetrised)
+// G = V[:, 0:m]^T W[:, 0:m] on the host, kept across iterations in Gk
+// (leading dimension mmax): only the columns added since the last call are
+// computed, B = V[:, 0:m]^T W[:, g_valid:m], and mirrored into the rows, so
+// the matrix is symmetric by construction.
 pq_status DavidsonRun::rayleigh(int mm, std::vector<double> &G) {
-  PQ_TRY(tmp.ensure(sizeof(double) * (size_t)mm * mm));
-  const double one = 1.0, zero = 0.0;
-  PQ_CUBLAS_TRY(cublasDgemm(cb, CUBLAS_OP_T, CUBLAS_OP_N, mm, mm, (int)n, &one, V.as<double>(), (int)n, W.as<double>(),
-                            (int)n, &zero, tmp.as<double>(), mm));
+  if ((int)Gk.size() < mmax * mmax) Gk.assign((size_t)mmax * mmax, 0.0);
+  if (g_valid < mm) {
+    const int c0 = g_valid, nc = mm - c0;
+    PQ_TRY(tmp.ensure(sizeof(double) * (size_t)mm * nc));
+    PQ_TRY(tall_skinny(cb, CUBLAS_OP_T, n, mm, V.as<double>(), W.as<double>() + (size_t)c0 * n, n, nc,
+                       tmp.as<double>(), mm));
+    std::vector<double> B((size_t)mm * nc);
+    PQ_CUDA_TRY(cudaMemcpyAsync(B.data(), tmp.ptr, sizeof(double) * mm * nc, cudaMemcpyDeviceToHost, st));
+    PQ_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int j = 0; j < nc; j++)
+      for (int i = 0; i < mm; i++) {
+        double v = B[i + (size_t)j * mm];
+        if (i >= c0 && i - c0 < j) continue;                                   // lower part of the new block
+        if (i >= c0 && i - c0 > j) v = 0.5 * (v + B[(c0 + j) + (size_t)(i - c0) * mm]);  // new x new: average
+        Gk[i + (size_t)(c0 + j) * mmax] = Gk[(c0 + j) + (size_t)i * mmax] = v;
+      }
+    g_valid = mm;
+  }
   G.resize((size_t)mm * mm);
-  PQ_CUDA_TRY(cudaMemcpyAsync(G.data(), tmp.ptr, sizeof(double) * mm * mm, cudaMemcpyDeviceToHost, st));
-  PQ_CUDA_TRY(cudaStreamSynchronize(st));
-  for (int i = 0; i < mm; i++)
-    for (int j = i + 1; j < mm; j++) {
-      double s = 0.5 * (G[i + (size_t)j * mm] + G[j + (size_t)i * mm]);
-      G[i + (size_t)j * mm] = G[j + (size_t)i * mm] = s;
-    }
+  for (int j = 0; j < mm; j++)
+    for (int i = 0; i < mm; i++) G[i + (size_t)j * mm] = Gk[i + (size_t)j * mmax];
   return PQ_OK;
 }
 
@@ -384,12 +412,16 @@ pq_status DavidsonRun::orthonormalize_append(int mm0, int kk, int *added) {
     double nrm0 = 0.0;
     PQ_CUBLAS_TRY(cublasDnrm2(cb, (int)n, t, 1, &nrm0));
     if (!(nrm0 > 0.0) || !std::isfinite(nrm0)) continue;
+    // classical Gram-Schmidt, repeated once unless the first pass kept at
+    // least 1/sqrt(2) of the norm (then t is orthogonal to working precision)
+    double nrm = nrm0;
     for (int pass = 0; pass < 2; pass++) {
+      const double before = nrm;
       PQ_CUBLAS_TRY(cublasDgemv(cb, CUBLAS_OP_T, (int)n, mm, &one, V.as<double>(), (int)n, t, 1, &zero, coef.as<double>(), 1));
       PQ_CUBLAS_TRY(cublasDgemv(cb, CUBLAS_OP_N, (int)n, mm, &mone, V.as<double>(), (int)n, coef.as<double>(), 1, &one, t, 1));
+      PQ_CUBLAS_TRY(cublasDnrm2(cb, (int)n, t, 1, &nrm));
+      if (nrm >= 0.70710678118654752 * before) break;
     }
-    double nrm = 0.0;
-    PQ_CUBLAS_TRY(cublasDnrm2(cb, (int)n, t, 1, &nrm));
     if (!(nrm > 1e-8 * nrm0) || nrm < 1e-300) continue;
     double inv = 1.0 / nrm;
     PQ_CUBLAS_TRY(cublasDscal(cb, (int)n, &inv, t, 1));

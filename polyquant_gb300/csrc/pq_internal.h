@@ -178,7 +178,8 @@ class DavidsonRun {
   ::cublasContext *cb = nullptr;
   bool own_cb = false;
   DevBuf V, W, X, R, T, tmp, dth, didx, coef;
-  std::vector<double> Z;
+  std::vector<double> Z, Gk;  // Ritz rotation; Rayleigh matrix (mmax x mmax, first g_valid columns valid)
+  int g_valid = 0;
   int k = 0, m0 = 0, mmax = 0, m = 0, it = 0, r_restart = 0;
   double tol = 1e-6, switch_tol = 1e-5, shift = 0.0, last_refined = 1e300, best32 = 1e300;
   int stall32 = 0;
