@@ -38,7 +38,9 @@ namespace pq {
 namespace batch {
 
 constexpr int JMAX = 5;             // columns per lane: rows of at most 160 values
-constexpr int MAXROW = 32 * JMAX;   // staging values per warp
+constexpr int MAXROW = 32 * JMAX;   // staging values per warp (group path)
+constexpr int LANE_MAXL = 16;       // widest row of the one-lane-per-row path
+constexpr int STAGE = 32 * LANE_MAXL > MAXROW ? 32 * LANE_MAXL : MAXROW;  // staging values per warp
 constexpr int MAX_P = 40;           // positron determinants (rows of 40 * 4 values)
 
 template <typename T> struct ProbT {
@@ -66,6 +68,7 @@ struct Prob {
 // Per-problem arguments of one batched sigma launch.
 struct Call {
   int active, precision, lw, cnt;  // lw = log2 of the padded width w; cnt <= w real columns
+  int lane_rows;                   // 1: one lane per row (rows of <= 16 values), 0: lane groups per row
   double shift;                    // FP32: sigma of (H - shift), added back in FP64
   void *X, *Y;                     // interleaved work vectors [det][w]
   const double *src;               // column-major FP64 input (leading dimension n_dets)
@@ -317,9 +320,182 @@ __device__ void do_rows(const Prob &p, const Call &cl, const Unit &U, T *stg, in
   }
 }
 
+// Narrow rows (L = P * w <= 16 values): one lane per row, so 32 rows of the
+// unit advance together.  The alpha-side connections are warp-uniform (same
+// alpha string) and their partner rows (Ja, Ib..Ib+31) are consecutive in
+// memory; the beta-side and alpha-beta connections are per lane.  Positron and
+// cross terms use the lane's own staging slot (no cross-lane traffic).
+template <typename T, int LV>
+__device__ void do_rows_lane(const Prob &p, const Call &cl, const Unit &U, T *stg, int lane) {
+  const ProbT<T> &q = pt<T>(p);
+  const int P = p.P, lw = cl.lw, L = P << lw;
+  const T *__restrict__ X = (const T *)cl.X;
+  T *__restrict__ Y = (T *)cl.Y;
+  const int ia = U.ia, nb = p.nb, npe = p.npe, npp = p.npp;
+  const int64_t a1b = p.a1_off[ia];
+  const int a1n = (int)(p.a1_off[ia + 1] - a1b);
+  const int64_t a2b = p.a2_off[ia];
+  const int a2n = (int)(p.a2_off[ia + 1] - a2b);
+  const uint64_t amask = p.astr[ia];
+  const T cf = (T)p.cf;
+  const int rowa = ia * nb;
+  T *slot = stg + lane * LV;  // this lane's staging slot
+  for (int r0 = 0; r0 < U.nrows; r0 += 32) {
+    const bool rok = r0 + lane < U.nrows;
+    const int ib = rok ? U.b0 + r0 + lane : U.b0;
+    const int Ie = rowa + ib;
+    const int64_t b1b = p.b1_off[ib];
+    const int b1n = rok ? (int)(p.b1_off[ib + 1] - b1b) : 0;
+    const int64_t b2b = p.b2_off[ib];
+    const int b2n = rok ? (int)(p.b2_off[ib + 1] - b2b) : 0;
+    const uint64_t bmask = p.bstr[ib];
+    T acc[LV];
+    {
+      const T *xr = X + (int64_t)Ie * L;
+      const double *dg = p.diag + (int64_t)Ie * P;
+#pragma unroll
+      for (int c = 0; c < LV; c++) {
+        acc[c] = T(0);
+        if (c < L) {
+          const T x = xr[c];
+          acc[c] = (T)(dg[c >> lw] - cl.shift) * x;
+          if (P > 1) slot[c] = x;
+        }
+      }
+    }
+    if (P > 1) {
+      const T *dea = q.dea + (int64_t)ia * 2 * npp, *deb = q.deb + (int64_t)ib * 2 * npp;
+#pragma unroll
+      for (int c = 0; c < LV; c++) {
+        if (c >= L) continue;
+        const int Jp = c >> lw, v = c & ((1 << lw) - 1);
+        T s = T(0);
+        for (int e = p.ps_off[Jp]; e < p.ps_off[Jp + 1]; e++) {
+          const int code = p.ps_code[e];
+          const int Ip = code & 255, y = (code >> 8) & 1, prs = code >> 10;
+          const T de = dea[y * npp + prs] + deb[y * npp + prs];
+          const T t = q.ps_h[e] + ((code >> 9) & 1 ? -cf : cf) * de;
+          s += t * slot[(Ip << lw) + v];
+        }
+        for (int e = p.pd_off[Jp]; e < p.pd_off[Jp + 1]; e++) s += q.pd_h[e] * slot[(p.pd_I[e] << lw) + v];
+        acc[c] += s;
+      }
+    }
+    // electron singles
+#pragma unroll 1
+    for (int x = 0; x < 2; x++) {
+      const int n1 = x == 0 ? a1n : b1n;
+      for (int t = 0; t < n1; t++) {
+        int info, Jr;
+        T f;
+        if (x == 0) {
+          const int64_t e = a1b + t;
+          info = p.a1_info[e];
+          f = q.a1F[e];
+          const T *er = q.eab + (int64_t)(info >> 1) * npe;
+          for (uint64_t m = bmask; m; m &= m - 1) f += er[pairdiag(__ffsll((long long)m) - 1)];
+          Jr = p.a1_J[e] * nb + ib;
+        } else {
+          const int64_t e = b1b + t;
+          info = p.b1_info[e];
+          f = q.b1F[e];
+          for (uint64_t m = amask; m; m &= m - 1)
+            f += q.eab[(int64_t)pairdiag(__ffsll((long long)m) - 1) * npe + (info >> 1)];
+          Jr = rowa + p.b1_J[e];
+        }
+        const T val = (info & 1) ? -f : f;
+        const T *xr = X + (int64_t)Jr * L;
+        if (P == 1) {
+#pragma unroll
+          for (int c = 0; c < LV; c++)
+            if (c < L) acc[c] += val * xr[c];
+        } else {
+          const int ph = info >> 1;
+          const T sc = (info & 1) ? -cf : cf;
+          T xv[LV];
+#pragma unroll
+          for (int c = 0; c < LV; c++) {
+            xv[c] = c < L ? xr[c] : T(0);
+            if (c < L) slot[c] = xv[c];
+          }
+          const T *dpt = q.dpt + ((int64_t)x * npe + ph) * P;
+          const T *epx0 = q.ep[x][0] + (int64_t)ph * npp, *epx1 = q.ep[x][1] + (int64_t)ph * npp;
+#pragma unroll
+          for (int c = 0; c < LV; c++) {
+            if (c >= L) continue;
+            const int Jp = c >> lw, v = c & ((1 << lw) - 1);
+            T s = (val + sc * dpt[Jp]) * xv[c];
+            for (int e = p.ps_off[Jp]; e < p.ps_off[Jp + 1]; e++) {
+              const int code = p.ps_code[e];
+              const int Ip = code & 255, prs = code >> 10;
+              const T ev = ((code >> 8) & 1) ? epx1[prs] : epx0[prs];
+              s += (((code >> 9) & 1) ? -sc : sc) * ev * slot[(Ip << lw) + v];
+            }
+            acc[c] += s;
+          }
+        }
+      }
+    }
+    // same-spin doubles
+#pragma unroll 1
+    for (int x = 0; x < 2; x++) {
+      const int n2 = x == 0 ? a2n : b2n;
+#pragma unroll 2
+      for (int t = 0; t < n2; t++) {
+        T val;
+        int Jr;
+        if (x == 0) {
+          val = q.a2D[a2b + t];
+          Jr = p.a2_J[a2b + t] * nb + ib;
+        } else {
+          val = q.b2D[b2b + t];
+          Jr = rowa + p.b2_J[b2b + t];
+        }
+        const T *xr = X + (int64_t)Jr * L;
+#pragma unroll
+        for (int c = 0; c < LV; c++)
+          if (c < L) acc[c] += val * xr[c];
+      }
+    }
+    // opposite-spin doubles
+#pragma unroll 1
+    for (int s = 0; s < a1n; s++) {
+      const int64_t ea = a1b + s;
+      const int infa = p.a1_info[ea];
+      const int rowj = p.a1_J[ea] * nb;
+      const T *erow = q.eab + (int64_t)(infa >> 1) * npe;
+#pragma unroll 2
+      for (int t = 0; t < b1n; t++) {
+        const int infb = p.b1_info[b1b + t];
+        const T v = erow[infb >> 1];
+        const T val = ((infa ^ infb) & 1) ? -v : v;
+        const T *xr = X + (int64_t)(rowj + p.b1_J[b1b + t]) * L;
+#pragma unroll
+        for (int c = 0; c < LV; c++)
+          if (c < L) acc[c] += val * xr[c];
+      }
+    }
+    if (rok) {
+      T *yr = Y + (int64_t)Ie * L;
+#pragma unroll
+      for (int c = 0; c < LV; c++)
+        if (c < L) yr[c] = acc[c];
+    }
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ void do_unit(const Prob &p, const Call &cl, const Unit &U, T *stg, int lane) {
   const int L = p.P << cl.lw;
+  if (cl.lane_rows) {
+    if (L <= 4)
+      do_rows_lane<T, 4>(p, cl, U, stg, lane);
+    else if (L <= 8)
+      do_rows_lane<T, 8>(p, cl, U, stg, lane);
+    else
+      do_rows_lane<T, 16>(p, cl, U, stg, lane);
+    return;
+  }
   const int G = L >= 32 ? 32 : (L <= 1 ? 1 : 1 << (32 - __clz(L - 1)));
   switch ((L + G - 1) / G) {
     case 1: do_rows<T, 1>(p, cl, U, stg, lane, G); break;
@@ -336,7 +512,7 @@ __global__ void __launch_bounds__(256) batch_sigma_kernel(const Prob *__restrict
                                                           unsigned *counter) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned char *stg = smem + (size_t)warp * MAXROW * sizeof(double);
+  unsigned char *stg = smem + (size_t)warp * STAGE * sizeof(double);
   for (;;) {
     unsigned u = 0;
     if (lane == 0) u = atomicAdd(counter, 1u);
@@ -686,6 +862,9 @@ double row_cost(const pq_ci_handle *h, const Prob &pr, int w) {
   return conn * std::max(L, 8.0) + (pr.P > 1 ? (s1a + s1b) * L * 10.0 : 0.0);
 }
 
+// one lane per determinant row when the widest row of the problem is narrow
+int lane_rows(const pq_ci_batch *B, int pi) { return B->prob[pi].P * B->wmax <= LANE_MAXL ? 1 : 0; }
+
 // Work units of a group: rows (ia, b0 .. b0 + nrows) in descending cost order.
 pq_status make_plan(pq_ci_batch *B, const std::vector<int> &members, int warps, int rows_mult, BatchPlan &pl) {
   struct U {
@@ -698,7 +877,7 @@ pq_status make_plan(pq_ci_batch *B, const std::vector<int> &members, int warps, 
     const Prob &pr = B->prob[pi];
     const int L = pr.P * B->wmax;
     const int G = L >= 32 ? 32 : (L <= 1 ? 1 : 1 << (32 - __builtin_clz((unsigned)(L - 1))));
-    const int nrows = (32 / G) * rows_mult;
+    const int nrows = (lane_rows(B, pi) ? 32 : 32 / G) * rows_mult;
     const double rc = row_cost(B->h[pi], pr, B->wmax);
     for (int ia = 0; ia < pr.na; ia++)
       for (int b0 = 0; b0 < pr.nb; b0 += nrows) {
@@ -720,7 +899,7 @@ pq_status make_plan(pq_ci_batch *B, const std::vector<int> &members, int warps, 
   PQ_TRY(upload(pl.units, uv, B->stream));
   PQ_TRY(upload(pl.chunks, ch, B->stream));
   pl.warps = warps;
-  const size_t smem = (size_t)warps * MAXROW * sizeof(double);
+  const size_t smem = (size_t)warps * STAGE * sizeof(double);
   int per_sm = 0;
   PQ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_sigma_kernel, warps * 32, smem));
   int dev = 0, sms = 0;
@@ -734,7 +913,7 @@ pq_status make_plan(pq_ci_batch *B, const std::vector<int> &members, int warps, 
 pq_status launch_sigma(pq_ci_batch *B, const BatchPlan &pl, const Unit *units, int n_units) {
   PQ_CUDA_TRY(cudaMemsetAsync(B->d_counter.ptr, 0, sizeof(unsigned), B->stream));
   if (n_units > 0) {
-    const size_t smem = (size_t)pl.warps * MAXROW * sizeof(double);
+    const size_t smem = (size_t)pl.warps * STAGE * sizeof(double);
     batch_sigma_kernel<<<pl.blocks, pl.warps * 32, smem, B->stream>>>(B->d_prob.as<Prob>(), B->d_calls.as<Call>(),
                                                                        units, n_units, B->d_counter.as<unsigned>());
     PQ_CUDA_TRY(cudaGetLastError());
@@ -801,6 +980,7 @@ pq_status autotune(pq_ci_batch *B, const std::vector<int> &members) {
     pq_ci_handle *h = B->h[pi];
     Call &c = B->h_calls[pi];
     c.active = 1;
+    c.lane_rows = lane_rows(B, pi);
     c.precision = PQ_FP32;
     c.lw = B->wmax == 4 ? 2 : (B->wmax == 2 ? 1 : 0);
     c.cnt = B->wmax;
@@ -942,8 +1122,9 @@ pq_status pq_ci_batch_sigma(pq_ci_batch *b, const double *const *C, const int64_
   if (b->own_stream) PQ_CUDA_TRY(cudaDeviceSynchronize());  // order after the caller's work
   std::vector<int> members(n);
   std::iota(members.begin(), members.end(), 0);
-  if (!b->all) {
-    b->wmax = 4;
+  const int want = nvec >= 3 ? 4 : nvec;  // widest block of this call
+  if (!b->all || b->wmax != want) {
+    b->wmax = want;
     PQ_TRY(ensure_work(b, members));
     PQ_TRY(get_plan(b, members, b->all));
   }
@@ -954,6 +1135,7 @@ pq_status pq_ci_batch_sigma(pq_ci_batch *b, const double *const *C, const int64_
       pq_ci_handle *h = b->h[i];
       Call &cl = b->h_calls[i];
       cl.active = 1;
+      cl.lane_rows = lane_rows(b, i);
       cl.precision = precision;
       cl.lw = log2w(c);
       cl.cnt = c;
@@ -1022,7 +1204,7 @@ pq_status pq_ci_batch_davidson(pq_ci_batch *b, const pq_davidson_params *p, size
     ~CbGuard() { cublasDestroy(c); }
   } guard{cb};
   pq_status overall = PQ_OK;
-  b->all.reset();  // the sigma-call plan assumed wmax = 4
+  b->all.reset();  // the sigma-call plan may assume another width
   for (const auto &grp : groups) {
     std::vector<std::unique_ptr<DavidsonRun>> runs;
     for (int pi : grp) {
@@ -1054,6 +1236,7 @@ pq_status pq_ci_batch_davidson(pq_ci_batch *b, const pq_davidson_params *p, size
           Call &cl = b->h_calls[grp[g]];
           const int c = std::min(b->wmax, r.req.cnt - v0);
           cl.active = 1;
+          cl.lane_rows = lane_rows(b, grp[g]);
           cl.precision = r.req.precision;
           cl.lw = log2w(c);
           cl.cnt = c;
