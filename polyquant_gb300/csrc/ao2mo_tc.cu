@@ -35,12 +35,16 @@ namespace tc {
 constexpr int BM = 128;          // output rows per CTA (TMEM lanes)
 constexpr int BN = 256;          // output columns per CTA (TMEM columns, UMMA N)
 constexpr int ROW_BYTES = 128;   // K extent of one stage, in bytes (one swizzle span)
-constexpr int STAGES = 2;
+// One stage of 96 KB keeps two CTAs resident per SM (2 x 256 TMEM columns), so
+// one CTA's loads and epilogue overlap the other's MMAs.
+constexpr int STAGES = 1;
 constexpr int A_TILE = BM * ROW_BYTES;  // 16 KB
 constexpr int B_TILE = BN * ROW_BYTES;  // 32 KB
 constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
-constexpr int TILE_LD = BN + 1;  // epilogue staging row stride (floats)
+constexpr int EPI_COLS = 128;        // accumulator columns per epilogue pass
+constexpr int TILE_LD = EPI_COLS + 1;  // epilogue staging row stride (floats)
+static_assert(BN % EPI_COLS == 0, "epilogue passes must tile the accumulator");
 static_assert(BM * TILE_LD * 4 <= STAGES * STAGE_BYTES, "epilogue tile must fit the stage buffers");
 constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
 
@@ -150,7 +154,7 @@ __device__ __forceinline__ float tf32_round(float x) {
 
 // TF32 = operands stored as FP32 (tf32-rounded); otherwise BF16.
 template <bool TF32, int EPI>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(128, 2)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant__ CUtensorMap tmA_lo,
                    const __grid_constant__ CUtensorMap tmB_hi, const __grid_constant__ CUtensorMap tmB_lo, GemmArgs g) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -251,44 +255,49 @@ __global__ void __launch_bounds__(128, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
   // Epilogue: TMEM -> shared tile (the stage buffers are idle once every MMA
-  // has completed) -> coalesced row stores by the whole CTA.
+  // has completed) -> coalesced row stores by the whole CTA, EPI_COLS
+  // accumulator columns per pass.
   float *tile = reinterpret_cast<float *>(smem);  // BM x TILE_LD floats (odd stride: conflict-free column writes)
-  if (acc_ok) {
-    const int r = warp * 32 + lane;
-    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-    for (int c0 = 0; c0 < BN; c0 += 32) {
-      float v[32];
-      tmem_ld32(taddr + c0, v);
+  for (int e0 = 0; e0 < BN; e0 += EPI_COLS) {
+    if (acc_ok) {
+      const int r = warp * 32 + lane;
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)e0;
+      for (int c0 = 0; c0 < EPI_COLS; c0 += 32) {
+        float v[32];
+        tmem_ld32(taddr + c0, v);
 #pragma unroll
-      for (int i = 0; i < 32; i++) tile[r * TILE_LD + c0 + i] = v[i];
-    }
-  }
-  __syncthreads();
-  if (acc_ok) {
-    for (int r = 0; r < BM; r++) {
-      const int m = mt * BM + r;
-      if (m >= g.M) break;
-      const float *trow = tile + r * TILE_LD;
-      if constexpr (EPI == EPI_SPLIT) {
-        const int64_t base = ((int64_t)b * g.M + m) * g.ld_out;
-        for (int n = threadIdx.x; n < g.N; n += 128) {
-          const float x = trow[n];
-          if constexpr (TF32) {
-            const float h = tf32_round(x);
-            static_cast<float *>(g.out_hi)[base + n] = h;
-            static_cast<float *>(g.out_lo)[base + n] = tf32_round(x - h);
-          } else {
-            const __nv_bfloat16 h = __float2bfloat16_rn(x);
-            static_cast<__nv_bfloat16 *>(g.out_hi)[base + n] = h;
-            static_cast<__nv_bfloat16 *>(g.out_lo)[base + n] = __float2bfloat16_rn(x - __bfloat162float(h));
-          }
-        }
-      } else {
-        float *out = g.out_pack + (int64_t)b * g.pack_stride + (int64_t)m * (m + 1) / 2;
-        const int lim = m + 1 < g.N ? m + 1 : g.N;
-        for (int n = threadIdx.x; n < lim; n += 128) out[n] = trow[n];
+        for (int i = 0; i < 32; i++) tile[r * TILE_LD + c0 + i] = v[i];
       }
     }
+    __syncthreads();
+    if (acc_ok) {
+      for (int r = 0; r < BM; r++) {
+        const int m = mt * BM + r;
+        if (m >= g.M) break;
+        const float *trow = tile + r * TILE_LD - e0;  // trow[n] for n in [e0, e0 + EPI_COLS)
+        const int nend = e0 + EPI_COLS < g.N ? e0 + EPI_COLS : g.N;
+        if constexpr (EPI == EPI_SPLIT) {
+          const int64_t base = ((int64_t)b * g.M + m) * g.ld_out;
+          for (int n = e0 + threadIdx.x; n < nend; n += 128) {
+            const float x = trow[n];
+            if constexpr (TF32) {
+              const float h = tf32_round(x);
+              static_cast<float *>(g.out_hi)[base + n] = h;
+              static_cast<float *>(g.out_lo)[base + n] = tf32_round(x - h);
+            } else {
+              const __nv_bfloat16 h = __float2bfloat16_rn(x);
+              static_cast<__nv_bfloat16 *>(g.out_hi)[base + n] = h;
+              static_cast<__nv_bfloat16 *>(g.out_lo)[base + n] = __float2bfloat16_rn(x - __bfloat162float(h));
+            }
+          }
+        } else {
+          float *out = g.out_pack + (int64_t)b * g.pack_stride + (int64_t)m * (m + 1) / 2;
+          const int lim = m + 1 < nend ? m + 1 : nend;
+          for (int n = e0 + threadIdx.x; n < lim; n += 128) out[n] = trow[n];
+        }
+      }
+    }
+    __syncthreads();
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -329,37 +338,36 @@ __device__ __forceinline__ int64_t tri64(int64_t i, int64_t j) { return i > j ? 
 // slice b of a pair-matrix source, split: S[b][nu][mu] = src(tri(mu,nu), b0 + b)
 // src64: column-major (ld x ncols) FP64 pair matrix (element (r, c) at r + c*ld)
 // src32: row-major FP32 pair rows (element (r, c) at c*ld + r), i.e. row c holds the slice
-// One block per slice; 32x32 tiles of the lower triangle are read with
-// consecutive pair indices (mu <= nu) and written to both triangles, the upper
-// one through a shared-memory transpose, so loads and stores are coalesced.
+// One block per (slice, 32x32 tile of the lower triangle): the tile is read
+// with consecutive pair indices (mu <= nu) and written to both triangles, the
+// upper one through a shared-memory transpose, so loads and stores are
+// coalesced and every slice spreads over many SMs.
 template <bool TF32>
 __global__ void __launch_bounds__(256) split_slices_kernel(const double *src64, const float *src32, int64_t ld, int n,
                                                            int ld_row, int64_t b0, typename Split<TF32>::T *hi,
                                                            typename Split<TF32>::T *lo) {
   __shared__ double tile[32][33];
+  const int nt = (n + 31) / 32;
+  const int tv = blockIdx.y / nt, tm = blockIdx.y - tv * nt;
+  if (tm > tv) return;
   const int64_t b = blockIdx.x, c = b0 + b;
   typename Split<TF32>::T *H = hi + b * (int64_t)n * ld_row, *L = lo + b * (int64_t)n * ld_row;
-  const int nt = (n + 31) / 32;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  for (int tv = 0; tv < nt; tv++)
-    for (int tm = 0; tm <= tv; tm++) {
-      for (int y = ty; y < 32; y += 8) {
-        const int nu = tv * 32 + y, mu = tm * 32 + tx;
-        double x = 0.0;
-        if (nu < n && mu <= nu) {
-          const int64_t pr = (int64_t)nu * (nu + 1) / 2 + mu;
-          x = src64 ? src64[pr + c * ld] : (double)src32[c * ld + pr];
-          Split<TF32>::run(x, H[(int64_t)nu * ld_row + mu], L[(int64_t)nu * ld_row + mu]);
-        }
-        tile[y][tx] = x;
-      }
-      __syncthreads();
-      for (int y = ty; y < 32; y += 8) {
-        const int mu = tm * 32 + y, nu = tv * 32 + tx;
-        if (nu < n && mu < nu) Split<TF32>::run(tile[tx][y], H[(int64_t)mu * ld_row + nu], L[(int64_t)mu * ld_row + nu]);
-      }
-      __syncthreads();
+  for (int y = ty; y < 32; y += 8) {
+    const int nu = tv * 32 + y, mu = tm * 32 + tx;
+    double x = 0.0;
+    if (nu < n && mu <= nu) {
+      const int64_t pr = (int64_t)nu * (nu + 1) / 2 + mu;
+      x = src64 ? src64[pr + c * ld] : (double)src32[c * ld + pr];
+      Split<TF32>::run(x, H[(int64_t)nu * ld_row + mu], L[(int64_t)nu * ld_row + mu]);
     }
+    tile[y][tx] = x;
+  }
+  __syncthreads();
+  for (int y = ty; y < 32; y += 8) {
+    const int mu = tm * 32 + y, nu = tv * 32 + tx;
+    if (nu < n && mu < nu) Split<TF32>::run(tile[tx][y], H[(int64_t)mu * ld_row + nu], L[(int64_t)mu * ld_row + nu]);
+  }
 }
 
 // full column-major pair matrix from the 8-fold packed vector: one block per
@@ -512,8 +520,9 @@ static pq_status ao2mo_tc_impl(const double *eri_ao, int layout, int64_t n, cons
   auto half = [&](const double *src64, const float *src32, int64_t ld_src, int64_t nslices, float *out) -> pq_status {
     for (int64_t b0 = 0; b0 < nslices; b0 += bt) {
       const int nb = (int)std::min(bt, nslices - b0);
-      tc::split_slices_kernel<TF32><<<(unsigned)nb, 256, 0, st>>>(src64, src32, ld_src, (int)n, ld, b0, sh.as<E>(),
-                                                                  sl.as<E>());
+      const unsigned ntile = (unsigned)((n + 31) / 32);
+      tc::split_slices_kernel<TF32><<<dim3((unsigned)nb, ntile * ntile), 256, 0, st>>>(src64, src32, ld_src, (int)n, ld,
+                                                                                      b0, sh.as<E>(), sl.as<E>());
       PQ_CUDA_TRY(cudaGetLastError());
       // GEMM 1: U^T[b] (nm x n) = Ct (nm x n) . S[b]^T, K = n
       Operand S{sh.ptr, sl.ptr, (int64_t)nb * n, ld};
