@@ -211,12 +211,40 @@ def bench_ao2mo(n=256, L=1024, seed=0):
         del r, d
     out["fp64"] = {"ms": ms64, "tflops": flops / (ms64 * 1e-3) / 1e12}
     b = out["bf16x3"]
+    cpu = cpu_ao2mo_sample(n, L, seed, synthetic.mo_coefficients(n, n, seed=seed + 1), flops)
     return {"metric": "AO->MO TFLOP/s", "value": b["tflops"], "unit": "TFLOP/s", "mode": "bf16x3",
             "workload": f"N_AO = N_MO = {n}, L = {L}, 8-fold packed FP64 input, seed {seed}",
             "algorithmic_flops": flops, "modes": out,
             "roofline": {"bound": "tensor", "achieved": b["tflops"], "peak": peak, "unit": "TFLOP/s",
                          "frac": b["tflops"] / peak, "peak_source": src,
-                         "note": "algorithmic flops; the split modes issue 3 MMAs per product"}}
+                         "note": "algorithmic flops; the split modes issue 3 MMAs per product"},
+            "cpu_baseline": cpu}
+
+
+def cpu_ao2mo_sample(n, L, seed, C, flops, n_sample=1024):
+    """FP64 numpy (host BLAS, all cores) time of the same pair-symmetric transform, extrapolated from a sample of
+    n_sample slices T = C^T S C of the first half transform to all 2 * n(n+1)/2 slices."""
+    from polyquant_gb300 import synthetic
+
+    Bp = synthetic.ao_eri_pairs(n, seed=seed, L=L)
+    npair = Bp.shape[1]
+    i, j = synthetic.pair_index(n)
+    cols = np.linspace(0, npair - 1, n_sample).astype(np.int64)
+    slices = []
+    for c in cols:
+        v = Bp.T @ Bp[:, c]
+        S = np.zeros((n, n))
+        S[i, j] = v
+        S[j, i] = v
+        slices.append(S)
+    t0 = time.perf_counter()
+    for S in slices:
+        T = C.T @ S @ C
+    dt = time.perf_counter() - t0
+    total = dt / n_sample * 2 * npair
+    return {"value": flops / total / 1e12, "unit": "TFLOP/s", "seconds_extrapolated": total, "cores": os.cpu_count(),
+            "kind": "port", "sample": f"{n_sample} of {2 * npair} slices (T = C^T S C, numpy FP64 BLAS), "
+                                      f"{dt:.2f} s, extrapolated"}
 
 
 def bench_psh_like(seed=0):
@@ -260,7 +288,7 @@ def bench_psh_like(seed=0):
     return res
 
 
-def bench_batch(n_problems=256, seed=0, roots=2, nsub=4, max_subspace=8, tol=1e-5):
+def bench_batch(n_problems=256, seed=0, roots=2, nsub=4, max_subspace=0, tol=1e-5):
     """Batched uneven CI: n_problems full-CI problems drawn by synthetic.batch_specs (n_orb ~ U{8..14},
     n_alpha, n_beta ~ U{2..n_orb//2}, 0-2 positrons in 6 orbitals, per-problem seeds), 2 roots each, solved
     by the lockstep batched Davidson (one persistent sigma launch per iteration, CUDA graph, autotuned launch
@@ -285,7 +313,7 @@ def bench_batch(n_problems=256, seed=0, roots=2, nsub=4, max_subspace=8, tol=1e-
                     "count_over_1e6": int((sizes > 1_000_000).sum())},
            "residual_tol": tol, "max_subspace": max_subspace}
     out = {}
-    for name, prec in (("fp64", PQ_FP64), ("mixed", PQ_FP32)):
+    for name, prec in (("mixed", PQ_FP32), ("fp64", PQ_FP64)):
         t0 = time.perf_counter()
         e, info = b.davidson(num_states=roots, num_subspace_vec=nsub, convergence_E=tol, precision=prec,
                              max_subspace=max_subspace)
@@ -299,7 +327,11 @@ def bench_batch(n_problems=256, seed=0, roots=2, nsub=4, max_subspace=8, tol=1e-
                      "sigma_seconds": float(max(i["sigma_seconds"] for i in info))}
     err = np.abs(out["mixed"] - out["fp64"]).max(axis=1)
     res["energy_error_mixed_vs_fp64"] = {"max": float(err.max()), "median": float(np.median(err)),
-                                         "count_over_1uEh": int((err > 1e-6).sum())}
+                                         "count_over_1uEh": int((err > 1e-6).sum()),
+                                         "over_1uEh": [{"problem": int(i), "dets": int(sizes[i]), "spec": specs[i],
+                                                        "fp64": out["fp64"][i].tolist(),
+                                                        "mixed": out["mixed"][i].tolist()}
+                                                       for i in np.nonzero(err > 1e-6)[0]]}
     res["tuning"] = b.tuning()
     b.close()
     return res
@@ -337,6 +369,7 @@ def main():
     ap.add_argument("--no-ao2mo", action="store_true")
     ap.add_argument("--no-psh", action="store_true")
     ap.add_argument("--only-ao2mo", action="store_true", help="run only the AO->MO measurement (profiling case)")
+    ap.add_argument("--ao2mo-n", type=int, default=256, help="AO/MO count of the AO->MO measurement (smaller: profiling)")
     ap.add_argument("--tts", action="store_true", help="also measure time to 1 uEh (FP64 vs mixed Davidson)")
     ap.add_argument("--batch", action="store_true", help="also run the batched uneven-CI workload")
     ap.add_argument("--only-batch", action="store_true", help="run only the batched uneven-CI workload")
@@ -354,7 +387,7 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     if args.only_ao2mo:
-        print(json.dumps(bench_ao2mo()), flush=True)
+        print(json.dumps(bench_ao2mo(n=args.ao2mo_n)), flush=True)
         return
     if args.only_batch:
         print(json.dumps({"batched_ci": bench_batch(args.batch_problems)}), flush=True)

@@ -11,14 +11,15 @@
 // accumulation in tensor memory (three MMAs per K step).  BF16 and TF32 keep
 // FP32's 8-bit exponent, so no per-block scaling is needed for range.
 //
-// GEMM kernel: one CTA (128 threads) per 128 x 256 output tile.  Thread 0
-// issues TMA tile loads (128-byte swizzle, two stages of K = 128 bytes of
-// each of A_hi, A_lo, B_hi, B_lo) and the tcgen05.mma instructions; the
-// accumulator (128 lanes x 256 FP32 columns) lives in TMEM; all four warps
-// read it back with tcgen05.ld for the epilogue (BF16/TF32 split of the
+// GEMM kernel: persistent, one CTA per SM looping over 128 x 256 output
+// tiles, warp-specialised: one thread issues TMA tile loads (128-byte
+// swizzle, a ring of two stages of K = 128 bytes of each of A_hi, A_lo, B_hi,
+// B_lo), one thread issues the tcgen05.mma instructions into one of two TMEM
+// accumulators (128 lanes x 256 FP32 columns each), and four warps drain the
+// other accumulator with tcgen05.ld for the epilogue (BF16/TF32 split of the
 // result for the next GEMM, or the packed lower triangle).  Every mbarrier
 // wait is bounded; a wait that runs out records an error code and the kernel
-// winds down (waits, bounded again, for its own loads, frees TMEM, returns).
+// winds down (waits, bounded again, for its own loads and MMAs, frees TMEM).
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -35,17 +36,19 @@ namespace tc {
 constexpr int BM = 128;          // output rows per CTA (TMEM lanes)
 constexpr int BN = 256;          // output columns per CTA (TMEM columns, UMMA N)
 constexpr int ROW_BYTES = 128;   // K extent of one stage, in bytes (one swizzle span)
-// One stage of 96 KB keeps two CTAs resident per SM (2 x 256 TMEM columns), so
-// one CTA's loads and epilogue overlap the other's MMAs.
-constexpr int STAGES = 1;
+// Persistent warp-specialised GEMM: one CTA per SM, a ring of two 96 KB
+// operand stages, and two TMEM accumulators (2 x 256 columns) so the epilogue
+// of one tile overlaps the loads and MMAs of the next.
+constexpr int STAGES = 2;
 constexpr int A_TILE = BM * ROW_BYTES;  // 16 KB
 constexpr int B_TILE = BN * ROW_BYTES;  // 32 KB
 constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
-constexpr int EPI_COLS = 128;        // accumulator columns per epilogue pass
-constexpr int TILE_LD = EPI_COLS + 1;  // epilogue staging row stride (floats)
-static_assert(BN % EPI_COLS == 0, "epilogue passes must tile the accumulator");
-static_assert(BM * TILE_LD * 4 <= STAGES * STAGE_BYTES, "epilogue tile must fit the stage buffers");
+constexpr int EPI_WARPS = 4;
+constexpr int EPI_LD = 33;                                  // per-warp 32 x 32 staging, odd stride
+constexpr int EPI_BYTES = EPI_WARPS * 32 * EPI_LD * 4;      // 16.5 KB
+constexpr int NBARS = 2 * STAGES + 4 + 1;                   // full, empty, acc_full[2], acc_empty[2], drain
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + EPI_BYTES + 1024 /*align*/ + 256 /*barriers, slots*/;
+constexpr int GEMM_THREADS = 64 + 32 * EPI_WARPS;           // producer warp, MMA warp, epilogue warps
 constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
 
 enum { EPI_SPLIT = 0, EPI_PACK = 1 };
@@ -54,6 +57,7 @@ enum { ERR_TIMEOUT_FULL = 1, ERR_TIMEOUT_MMA = 2, ERR_TIMEOUT_ACC = 3 };
 struct GemmArgs {
   int M, N, K;                 // logical sizes
   int m_tiles;                 // ceil(M / BM)
+  int nbatch;                  // batch entries (tiles = nbatch * m_tiles)
   int a_batched, b_batched;    // operand varies with the batch index
   int a_rows, b_rows;          // rows per batch in the operand tensors
   int ld_out;                  // EPI_SPLIT: row length of the split output
@@ -70,6 +74,9 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
 }
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
   uint32_t ok;
@@ -153,32 +160,52 @@ __device__ __forceinline__ float tf32_round(float x) {
 }
 
 // TF32 = operands stored as FP32 (tf32-rounded); otherwise BF16.
+// Roles: warp 0 lane 0 issues TMA loads into the stage ring, warp 1 lane 0
+// issues the MMAs (tile i into accumulator i & 1), warps 2..5 drain the
+// accumulators (warp w reads TMEM lanes 32 (w & 3) .. + 31) through a
+// per-warp shared-memory staging block into coalesced row stores.  Barriers:
+// full[s] (loads landed), empty[s] (MMAs reading stage s done), acc_full[a]
+// (tile's MMAs done), acc_empty[a] (epilogue done with accumulator a).  Every
+// wait is bounded; a wait that runs out sets the error word and an abort flag
+// that every role polls, the producer then waits (bounded) for its own loads
+// in flight, the MMA thread for its own MMAs, and the CTA frees TMEM.
 template <bool TF32, int EPI>
-__global__ void __launch_bounds__(128, 2)
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant__ CUtensorMap tmA_lo,
                    const __grid_constant__ CUtensorMap tmB_hi, const __grid_constant__ CUtensorMap tmB_lo, GemmArgs g) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1024-byte alignment of the shared-window address (128-byte swizzle atoms)
   unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE_BYTES);
-  // bars[0..STAGES): tiles loaded; bars[STAGES..2*STAGES): MMAs of a stage done; bars[2*STAGES]: accumulator ready
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * STAGES + 1);
+  float *epi = reinterpret_cast<float *>(smem + STAGES * STAGE_BYTES);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE_BYTES + EPI_BYTES);
+  uint64_t *full = bars, *empty = bars + STAGES, *accf = bars + 2 * STAGES, *acce = bars + 2 * STAGES + 2;
+  uint64_t *drain = bars + 2 * STAGES + 4;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + NBARS);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int b = blockIdx.x / g.m_tiles, mt = blockIdx.x % g.m_tiles;
   constexpr int ESZ = TF32 ? 4 : 2;
-  constexpr int BK = ROW_BYTES / ESZ;         // K elements per stage
-  constexpr int UK = TF32 ? 8 : 16;           // K per MMA instruction
+  constexpr int BK = ROW_BYTES / ESZ;  // K elements per stage
+  constexpr int UK = TF32 ? 8 : 16;    // K per MMA instruction
   const int nst = (g.K + BK - 1) / BK;
+  const int n_tiles = g.nbatch * g.m_tiles;
 
   if (threadIdx.x == 0) {
-    for (int i = 0; i < 2 * STAGES + 1; i++) mbar_init(smem_u32(bars + i), 1);
+    for (int i = 0; i < STAGES; i++) {
+      mbar_init(smem_u32(full + i), 1);
+      mbar_init(smem_u32(empty + i), 1);
+    }
+    for (int a = 0; a < 2; a++) {
+      mbar_init(smem_u32(accf + a), 1);
+      mbar_init(smem_u32(acce + a), EPI_WARPS);
+    }
+    mbar_init(smem_u32(drain), 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)), "r"(BN)
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(2 * BN)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -186,122 +213,135 @@ __global__ void __launch_bounds__(128, 2)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  if (threadIdx.x == 0) {
-    const int ya = (g.a_batched ? b * g.a_rows : 0) + mt * BM;
-    const int yb = g.b_batched ? b * g.b_rows : 0;
+  if (warp == 0 && lane == 0) {
+    // ---- producer
+    int gs = 0;
+    for (int t = blockIdx.x; t < n_tiles && !*abort_flag; t += gridDim.x) {
+      const int b = t / g.m_tiles, mt = t - b * g.m_tiles;
+      const int ya = (g.a_batched ? b * g.a_rows : 0) + mt * BM;
+      const int yb = g.b_batched ? b * g.b_rows : 0;
+      for (int s = 0; s < nst; s++, gs++) {
+        const int slot = gs % STAGES;
+        const uint32_t ph = (uint32_t)((gs / STAGES) & 1);
+        if (!mbar_wait(smem_u32(empty + slot), ph ^ 1u)) {
+          atomicCAS(g.err, 0, ERR_TIMEOUT_MMA);
+          *abort_flag = 1;
+          break;
+        }
+        if (*abort_flag) break;
+        unsigned char *st = smem + slot * STAGE_BYTES;
+        const uint32_t bar = smem_u32(full + slot);
+        mbar_expect_tx(bar, STAGE_BYTES);
+        const int x = s * BK;
+        tma_load_2d(smem_u32(st), &tmA_hi, x, ya, bar);
+        tma_load_2d(smem_u32(st + A_TILE), &tmA_lo, x, ya, bar);
+        tma_load_2d(smem_u32(st + 2 * A_TILE), &tmB_hi, x, yb, bar);
+        tma_load_2d(smem_u32(st + 2 * A_TILE + B_TILE), &tmB_lo, x, yb, bar);
+      }
+    }
+    // the loads of the last stages must have landed before the CTA exits
+    for (int j = gs > STAGES ? gs - STAGES : 0; j < gs; j++)
+      mbar_wait(smem_u32(full + (j % STAGES)), (uint32_t)((j / STAGES) & 1));
+  } else if (warp == 1 && lane == 0) {
+    // ---- MMA issuer
     const uint32_t idesc = instr_desc(TF32 ? 2u : 1u);
-    int issued = 0;  // stages whose loads were issued
-    auto issue = [&](int s) {
-      const int buf = s % STAGES;
-      unsigned char *st = smem + buf * STAGE_BYTES;
-      const uint32_t bar = smem_u32(bars + buf);
-      mbar_expect_tx(bar, STAGE_BYTES);
-      const int x = s * BK;
-      tma_load_2d(smem_u32(st), &tmA_hi, x, ya, bar);
-      tma_load_2d(smem_u32(st + A_TILE), &tmA_lo, x, ya, bar);
-      tma_load_2d(smem_u32(st + 2 * A_TILE), &tmB_hi, x, yb, bar);
-      tma_load_2d(smem_u32(st + 2 * A_TILE + B_TILE), &tmB_lo, x, yb, bar);
-      issued = s + 1;
-    };
-    for (int s = 0; s < nst && s < STAGES; s++) issue(s);
-    bool ok = true;
-    for (int s = 0; s < nst && ok; s++) {
-      const int buf = s % STAGES;
-      const uint32_t par = (uint32_t)((s / STAGES) & 1);
-      if (!mbar_wait(smem_u32(bars + buf), par)) {
-        atomicCAS(g.err, 0, ERR_TIMEOUT_FULL);
-        ok = false;
+    int gs = 0, i = 0;
+    for (int t = blockIdx.x; t < n_tiles && !*abort_flag; t += gridDim.x, i++) {
+      const int a = i & 1;
+      const uint32_t aph = (uint32_t)((i >> 1) & 1);
+      if (!mbar_wait(smem_u32(acce + a), aph ^ 1u)) {
+        atomicCAS(g.err, 0, ERR_TIMEOUT_ACC);
+        *abort_flag = 1;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      unsigned char *st = smem + buf * STAGE_BYTES;
-      const uint32_t a_hi = smem_u32(st), a_lo = smem_u32(st + A_TILE);
-      const uint32_t b_hi = smem_u32(st + 2 * A_TILE), b_lo = smem_u32(st + 2 * A_TILE + B_TILE);
-#pragma unroll
-      for (int kk = 0; kk < BK / UK; kk++) {
-        const uint32_t off = kk * UK * ESZ;  // bytes along K inside the swizzle span
-        const uint32_t acc0 = (s > 0 || kk > 0) ? 1u : 0u;
-        mma<TF32>(tmem, smem_desc(a_hi + off), smem_desc(b_hi + off), idesc, acc0);
-        mma<TF32>(tmem, smem_desc(a_hi + off), smem_desc(b_lo + off), idesc, 1u);
-        mma<TF32>(tmem, smem_desc(a_lo + off), smem_desc(b_hi + off), idesc, 1u);
-      }
-      mma_commit(smem_u32(bars + STAGES + buf));
-      if (s + STAGES < nst) {
-        // the buffer is reloaded only after the MMAs reading it completed
-        if (!mbar_wait(smem_u32(bars + STAGES + buf), par)) {
-          atomicCAS(g.err, 0, ERR_TIMEOUT_MMA);
+      const uint32_t d = tmem + (uint32_t)(a * BN);
+      bool ok = true;
+      for (int s = 0; s < nst; s++, gs++) {
+        const int slot = gs % STAGES;
+        const uint32_t ph = (uint32_t)((gs / STAGES) & 1);
+        if (!mbar_wait(smem_u32(full + slot), ph)) {
+          atomicCAS(g.err, 0, ERR_TIMEOUT_FULL);
+          *abort_flag = 1;
           ok = false;
           break;
         }
-        issue(s + STAGES);
-      }
-    }
-    if (ok) {
-      mma_commit(smem_u32(bars + 2 * STAGES));
-    } else {
-      *abort_flag = 1;
-      // wind down: wait (bounded) for this CTA's own loads still in flight
-      for (int s = (issued > STAGES ? issued - STAGES : 0); s < issued; s++)
-        mbar_wait(smem_u32(bars + (s % STAGES)), (uint32_t)((s / STAGES) & 1));
-      mbar_try(smem_u32(bars + 2 * STAGES), 0);
-    }
-  }
-  __syncthreads();
-  bool acc_ok = (*abort_flag == 0);
-  if (acc_ok) {
-    acc_ok = mbar_wait(smem_u32(bars + 2 * STAGES), 0);
-    if (!acc_ok && lane == 0) atomicCAS(g.err, 0, ERR_TIMEOUT_ACC);
-  }
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-
-  // Epilogue: TMEM -> shared tile (the stage buffers are idle once every MMA
-  // has completed) -> coalesced row stores by the whole CTA, EPI_COLS
-  // accumulator columns per pass.
-  float *tile = reinterpret_cast<float *>(smem);  // BM x TILE_LD floats (odd stride: conflict-free column writes)
-  for (int e0 = 0; e0 < BN; e0 += EPI_COLS) {
-    if (acc_ok) {
-      const int r = warp * 32 + lane;
-      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)e0;
-      for (int c0 = 0; c0 < EPI_COLS; c0 += 32) {
-        float v[32];
-        tmem_ld32(taddr + c0, v);
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        unsigned char *st = smem + slot * STAGE_BYTES;
+        const uint32_t a_hi = smem_u32(st), a_lo = smem_u32(st + A_TILE);
+        const uint32_t b_hi = smem_u32(st + 2 * A_TILE), b_lo = smem_u32(st + 2 * A_TILE + B_TILE);
 #pragma unroll
-        for (int i = 0; i < 32; i++) tile[r * TILE_LD + c0 + i] = v[i];
-      }
-    }
-    __syncthreads();
-    if (acc_ok) {
-      for (int r = 0; r < BM; r++) {
-        const int m = mt * BM + r;
-        if (m >= g.M) break;
-        const float *trow = tile + r * TILE_LD - e0;  // trow[n] for n in [e0, e0 + EPI_COLS)
-        const int nend = e0 + EPI_COLS < g.N ? e0 + EPI_COLS : g.N;
-        if constexpr (EPI == EPI_SPLIT) {
-          const int64_t base = ((int64_t)b * g.M + m) * g.ld_out;
-          for (int n = e0 + threadIdx.x; n < nend; n += 128) {
-            const float x = trow[n];
-            if constexpr (TF32) {
-              const float h = tf32_round(x);
-              static_cast<float *>(g.out_hi)[base + n] = h;
-              static_cast<float *>(g.out_lo)[base + n] = tf32_round(x - h);
-            } else {
-              const __nv_bfloat16 h = __float2bfloat16_rn(x);
-              static_cast<__nv_bfloat16 *>(g.out_hi)[base + n] = h;
-              static_cast<__nv_bfloat16 *>(g.out_lo)[base + n] = __float2bfloat16_rn(x - __bfloat162float(h));
-            }
-          }
-        } else {
-          float *out = g.out_pack + (int64_t)b * g.pack_stride + (int64_t)m * (m + 1) / 2;
-          const int lim = m + 1 < nend ? m + 1 : nend;
-          for (int n = e0 + threadIdx.x; n < lim; n += 128) out[n] = trow[n];
+        for (int kk = 0; kk < BK / UK; kk++) {
+          const uint32_t off = kk * UK * ESZ;  // bytes along K inside the swizzle span
+          const uint32_t acc0 = (s > 0 || kk > 0) ? 1u : 0u;
+          mma<TF32>(d, smem_desc(a_hi + off), smem_desc(b_hi + off), idesc, acc0);
+          mma<TF32>(d, smem_desc(a_hi + off), smem_desc(b_lo + off), idesc, 1u);
+          mma<TF32>(d, smem_desc(a_lo + off), smem_desc(b_hi + off), idesc, 1u);
         }
+        mma_commit(smem_u32(empty + slot));  // frees the stage once these MMAs completed
       }
+      if (!ok) break;
+      mma_commit(smem_u32(accf + a));
     }
-    __syncthreads();
+    // every MMA issued by this thread has completed before TMEM is freed
+    mma_commit(smem_u32(drain));
+    mbar_wait(smem_u32(drain), 0);
+  } else if (warp >= 2) {
+    // ---- epilogue
+    const int q = warp & 3;  // TMEM lane quadrant of this warp
+    float *stg = epi + (warp - 2) * 32 * EPI_LD;
+    int i = 0;
+    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, i++) {
+      const int a = i & 1;
+      const uint32_t aph = (uint32_t)((i >> 1) & 1);
+      const bool ok = mbar_wait(smem_u32(accf + a), aph);
+      if (!ok || *abort_flag) {
+        if (!ok && lane == 0) atomicCAS(g.err, 0, ERR_TIMEOUT_ACC);
+        *abort_flag = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int b = t / g.m_tiles, mt = t - b * g.m_tiles;
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * BN);
+      const int row0 = mt * BM + q * 32;
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        float v[32];
+        tmem_ld32(taddr + c0, v);  // v[j] = D[row0 + lane][c0 + j]
+#pragma unroll
+        for (int j = 0; j < 32; j++) stg[lane * EPI_LD + j] = v[j];
+        __syncwarp();
+        const int n = c0 + lane;
+        for (int rr = 0; rr < 32; rr++) {
+          const int m = row0 + rr;
+          if (m >= g.M) break;
+          const float x = stg[rr * EPI_LD + lane];
+          if constexpr (EPI == EPI_SPLIT) {
+            if (n < g.N) {
+              const int64_t o = ((int64_t)b * g.M + m) * g.ld_out + n;
+              if constexpr (TF32) {
+                const float h = tf32_round(x);
+                static_cast<float *>(g.out_hi)[o] = h;
+                static_cast<float *>(g.out_lo)[o] = tf32_round(x - h);
+              } else {
+                const __nv_bfloat16 h = __float2bfloat16_rn(x);
+                static_cast<__nv_bfloat16 *>(g.out_hi)[o] = h;
+                static_cast<__nv_bfloat16 *>(g.out_lo)[o] = __float2bfloat16_rn(x - __bfloat162float(h));
+              }
+            }
+          } else {
+            if (n <= m && n < g.N) g.out_pack[(int64_t)b * g.pack_stride + (int64_t)m * (m + 1) / 2 + n] = x;
+          }
+        }
+        __syncwarp();
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(acce + a));
+    }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN) : "memory");
 }
 
 // ---------------------------------------------------------------------------
@@ -472,10 +512,15 @@ static pq_status run_gemm(const Operand &A, const Operand &B, bool a_batched, bo
   g.b_batched = b_batched;
   g.a_rows = M;
   g.b_rows = N;
+  g.nbatch = nbatch;
   auto kern = tc::tc_gemm_kernel<TF32, EPI>;
   PQ_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES));
-  const int64_t grid = (int64_t)nbatch * g.m_tiles;
-  kern<<<(unsigned)grid, 128, tc::SMEM_BYTES, st>>>(ma_hi, ma_lo, mb_hi, mb_lo, g);
+  int dev = 0, sms = 0;
+  PQ_CUDA_TRY(cudaGetDevice(&dev));
+  PQ_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t tiles = (int64_t)nbatch * g.m_tiles;
+  const int grid = (int)std::min<int64_t>(tiles, sms);  // persistent: one CTA per SM
+  kern<<<grid, tc::GEMM_THREADS, tc::SMEM_BYTES, st>>>(ma_hi, ma_lo, mb_hi, mb_lo, g);
   PQ_CUDA_TRY(cudaGetLastError());
   return PQ_OK;
 }
