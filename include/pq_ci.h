@@ -155,6 +155,36 @@ typedef struct {
 pq_status pq_ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *energies, double *vecs,
                          pq_davidson_report *report);
 
+/* ---- explicit sparse Hamiltonian ------------------------------------------
+ * Replaces POLYQUANT_DETSET::create_ham (src/ci/detset/explicit_ham.cpp:51-84,
+ * explicit_ham_singleparticle.cpp; the reference's default build_matrix path)
+ * and its use through Spectra::SparseSymMatProd (src/ci/epci.cpp:623-668).
+ * Builds H on the device (one species, FP64); exact zeros are dropped and,
+ * for screening_threshold > 0, every |H_IJ| <= threshold (the reference's
+ * ham.prune(threshold, 1.0)).  use_for_sigma != 0 makes FP64 sigma calls
+ * (pq_ci_sigma*, pq_ci_davidson's FP64 requests) multiply with the matrix;
+ * FP32 requests keep the direct kernels.  *nnz: stored entries (both
+ * triangles). */
+pq_status pq_ci_ham_build(pq_ci_handle *h, double screening_threshold, int32_t use_for_sigma, int64_t *nnz);
+pq_status pq_ci_ham_release(pq_ci_handle *h);
+
+/* Host copy in CSR: upper != 0 gives the reference's storage (upper triangle
+ * with the diagonal, row-major, columns ascending), else both triangles.
+ * row_ptr: n_dets + 1 entries; col/val: *nnz entries.  Pass NULL arrays to
+ * query *nnz first. */
+pq_status pq_ci_ham_csr(pq_ci_handle *h, int32_t upper, int64_t *nnz, int64_t *row_ptr, int32_t *col, double *val);
+
+/* ---- properties of CI vectors (one species) --------------------------------
+ * <S^2> of nvec states: replaces POLYQUANT_DETSET::evaluate_s2
+ * (src/ci/detset/s2.cpp:4-123).  C: DEVICE, n_dets x nvec column-major;
+ * s2: host, nvec values. */
+pq_status pq_ci_s2(pq_ci_handle *h, const double *C, int64_t ldc, int32_t nvec, double *s2);
+
+/* One-particle density matrix of one state and spin (0 alpha, 1 beta):
+ * replaces create_1rdm (src/ci/detset/rdm1.cpp:4-72).  C: DEVICE, n_dets
+ * values; rdm: host, n_orb x n_orb column-major. */
+pq_status pq_ci_rdm1(pq_ci_handle *h, const double *C, int32_t spin, double *rdm);
+
 /* ---- batches of independent problems -------------------------------------
  * Many small CI problems of uneven size solved together: one persistent sigma
  * kernel per Davidson iteration covers every active problem (work units

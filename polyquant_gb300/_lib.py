@@ -20,7 +20,8 @@ EXPORTS = [
     "pq_last_error", "pq_version", "pq_ci_create", "pq_ci_destroy", "pq_ci_num_dets", "pq_ci_strings",
     "pq_ci_det_unfold", "pq_ci_diag", "pq_ci_sigma", "pq_ci_sigma_host", "pq_ci_sigma_noalloc",
     "pq_ci_sigma_interleaved",
-    "pq_ci_davidson", "pq_ci_batch_create", "pq_ci_batch_destroy", "pq_ci_batch_num_dets", "pq_ci_batch_sigma",
+    "pq_ci_davidson", "pq_ci_ham_build", "pq_ci_ham_release", "pq_ci_ham_csr", "pq_ci_s2", "pq_ci_rdm1",
+    "pq_ci_batch_create", "pq_ci_batch_destroy", "pq_ci_batch_num_dets", "pq_ci_batch_sigma",
     "pq_ci_batch_tuning", "pq_ci_batch_davidson", "pq_ao2mo", "pq_mo1",
 ]
 
@@ -106,6 +107,16 @@ def load(path: str = LIB_PATH):
     L.pq_ci_sigma_interleaved.argtypes = [P, P, P, I32, I32, D]
     L.pq_ci_davidson.restype = I32
     L.pq_ci_davidson.argtypes = [P, ctypes.POINTER(PQDavidsonParams), P, P, ctypes.POINTER(PQDavidsonReport)]
+    L.pq_ci_ham_build.restype = I32
+    L.pq_ci_ham_build.argtypes = [P, D, I32, ctypes.POINTER(I64)]
+    L.pq_ci_ham_release.restype = I32
+    L.pq_ci_ham_release.argtypes = [P]
+    L.pq_ci_ham_csr.restype = I32
+    L.pq_ci_ham_csr.argtypes = [P, I32, ctypes.POINTER(I64), P, P, P]
+    L.pq_ci_s2.restype = I32
+    L.pq_ci_s2.argtypes = [P, P, I64, I32, P]
+    L.pq_ci_rdm1.restype = I32
+    L.pq_ci_rdm1.argtypes = [P, P, I32, P]
     L.pq_ci_batch_create.restype = I32
     L.pq_ci_batch_create.argtypes = [ctypes.POINTER(PQDesc), I32, P, ctypes.POINTER(P)]
     L.pq_ci_batch_destroy.restype = I32

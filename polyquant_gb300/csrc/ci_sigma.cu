@@ -19,6 +19,7 @@
 // fetches all roots of a determinant.
 #include <algorithm>
 
+#include "ci_conn.cuh"
 #include "pq_internal.h"
 
 namespace pq {
@@ -349,6 +350,7 @@ static pq_status sigma_dispatch(pq_ci_handle *h, const T *X, T *Y, double shift)
 pq_status ci_sigma_il(pq_ci_handle *h, const void *X, void *Y, int nvp, int precision, double shift,
                       bool allow_scratch) {
   if (h->n_species == 2) return ci_sigma2_il(h, X, Y, nvp, precision, shift);
+  if (h->use_explicit && precision == PQ_FP64 && shift == 0.0) return ci_ham_spmv(h, X, Y, nvp);
   if (precision == PQ_FP32 && allow_scratch && h->fp32_v2) return ci_sigma32_v2(h, X, Y, nvp, shift);
   if (precision == PQ_FP64) {
     if (nvp == 1) return sigma_dispatch<double, 1>(h, (const double *)X, (double *)Y, shift);
@@ -411,60 +413,15 @@ namespace pq {
 // Columns H[:, I_c] of the Hamiltonian for a list of determinants I_c (one
 // species), written into column-major W (zeroed by the caller): the exact
 // FP64 sigma of the unit vectors e_{I_c} from the connections of I_c alone.
-// Block c handles column c; its threads walk the connection list of I_c
-// (diagonal, alpha and beta singles, same-spin doubles, alpha-beta doubles).
-__global__ void unit_columns_kernel(SigmaArgs<double> a, const int32_t *cia, const int32_t *cib, int64_t n, double *W) {
+// Block c handles column c; its threads walk the connection list of I_c.
+__global__ void unit_columns_kernel(ConnArgs a, const int32_t *cia, const int32_t *cib, int64_t n, double *W) {
   const int c = blockIdx.x;
-  const int ia = cia[c], ib = cib[c];
   double *w = W + (int64_t)c * n;
-  const int64_t I = a.rowoff[ia] + ib;
-  const int64_t a1b = a.a.s1_off[ia], a2b = a.a.s2_off[ia], b1b = a.b.s1_off[ib], b2b = a.b.s2_off[ib];
-  const int n1a = (int)(a.a.s1_off[ia + 1] - a1b), n2a = (int)(a.a.s2_off[ia + 1] - a2b);
-  const int n1b = (int)(a.b.s1_off[ib + 1] - b1b), n2b = (int)(a.b.s2_off[ib + 1] - b2b);
-  const uint64_t am = a.a.str[ia], bm = a.b.str[ib];
-  const int64_t tot = 1 + (int64_t)n1a + n1b + n2a + n2b + (int64_t)n1a * n1b;
+  const ConnRow r = conn_row(a, cia[c], cib[c]);
+  const int64_t tot = r.total();
   for (int64_t t = threadIdx.x; t < tot; t += blockDim.x) {
-    int64_t J = -1;
-    double v = 0.0;
-    int64_t r = t;
-    if (r == 0) {
-      J = I;
-      v = a.diag[I];
-    } else if ((r -= 1) < n1a) {
-      const int Ja = a.a.s1_J[a1b + r], info = a.a.s1_info[a1b + r], ph = info >> 1;
-      double f = a.a.s1_F[a1b + r];
-      for (uint64_t m = bm; m; m &= m - 1) {
-        const int k = __ffsll((long long)m) - 1;
-        f += a.eab[(int64_t)ph * a.npair + k * (k + 3) / 2];
-      }
-      v = (info & 1) ? -f : f;
-      if (ib < a.rowlen[Ja]) J = a.rowoff[Ja] + ib;
-    } else if ((r -= n1a) < n1b) {
-      const int Jb = a.b.s1_J[b1b + r], info = a.b.s1_info[b1b + r], ph = info >> 1;
-      double f = a.b.s1_F[b1b + r];
-      for (uint64_t m = am; m; m &= m - 1) {
-        const int k = __ffsll((long long)m) - 1;
-        f += a.eab[(int64_t)(k * (k + 3) / 2) * a.npair + ph];
-      }
-      v = (info & 1) ? -f : f;
-      if (Jb < a.rowlen[ia]) J = a.rowoff[ia] + Jb;
-    } else if ((r -= n1b) < n2a) {
-      const int Ja = a.a.s2_J[a2b + r];
-      v = a.a.s2_D[a2b + r];
-      if (ib < a.rowlen[Ja]) J = a.rowoff[Ja] + ib;
-    } else if ((r -= n2a) < n2b) {
-      const int Jb = a.b.s2_J[b2b + r];
-      v = a.b.s2_D[b2b + r];
-      if (Jb < a.rowlen[ia]) J = a.rowoff[ia] + Jb;
-    } else {
-      r -= n2b;
-      const int s = (int)(r / n1b), q = (int)(r - (int64_t)s * n1b);
-      const int Ja = a.a.s1_J[a1b + s], ia_ = a.a.s1_info[a1b + s];
-      const int Jb = a.b.s1_J[b1b + q], ib_ = a.b.s1_info[b1b + q];
-      const double e = a.eab[(int64_t)(ia_ >> 1) * a.npair + (ib_ >> 1)];
-      v = ((ia_ ^ ib_) & 1) ? -e : e;
-      if (Jb < a.rowlen[Ja]) J = a.rowoff[Ja] + Jb;
-    }
+    double v;
+    const int64_t J = conn_elem(a, r, t, &v);
     if (J >= 0) w[J] = v;
   }
 }
@@ -486,14 +443,7 @@ pq_status ci_unit_columns(pq_ci_handle *h, const std::vector<int64_t> &dets, dou
   PQ_TRY(upload(dia, ia, h->stream));
   PQ_TRY(upload(dib, ib, h->stream));
   PQ_CUDA_TRY(cudaMemsetAsync(W, 0, sizeof(double) * (size_t)h->n_dets * m, h->stream));
-  SigmaArgs<double> a{};
-  a.a = make_view<double>(h->tab[0][0]);
-  a.b = make_view<double>(h->tab[0][1]);
-  a.rowoff = h->d_rowoff.as<int64_t>();
-  a.rowlen = h->d_rowlen.as<int32_t>();
-  a.eab = h->d_eab64.as<double>();
-  a.diag = h->d_diag.as<double>();
-  a.npair = h->npair[0];
+  const ConnArgs a = make_conn_args(h);
   unit_columns_kernel<<<m, 256, 0, h->stream>>>(a, dia.as<int32_t>(), dib.as<int32_t>(), h->n_dets, W);
   PQ_CUDA_TRY(cudaGetLastError());
   PQ_CUDA_TRY(cudaStreamSynchronize(h->stream));  // the index lists are freed on return

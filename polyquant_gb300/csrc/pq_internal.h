@@ -112,6 +112,10 @@ struct pq_ci_handle {
   pq::DevBuf d_e_a, d_e_b, d_ebase, d_elev, d_prowoff, d_prowlen, d_pfirst, d_psize, d_pdet_a, d_pdet_b;
   // integral blocks, row-major: [s] same-species alpha|beta, [se][sp] electron|positron
   pq::DevBuf d_eabs64[2], d_eabs32[2], d_ep64[2][2], d_ep32[2][2];
+  // explicit Hamiltonian (ci_explicit.cu): CSR with both triangles, FP64
+  pq::DevBuf d_hrow, d_hcol, d_hval;
+  int64_t h_nnz = 0;
+  bool use_explicit = false;  // FP64 sigma multiplies with the explicit matrix
 };
 
 namespace pq {
@@ -127,6 +131,8 @@ pq_status ci_unfold2(const pq_ci_handle *h, int32_t *out);
 // allow_scratch = false keeps sigma on kernels that need no work memory beyond X and Y
 pq_status ci_sigma_il(pq_ci_handle *h, const void *X, void *Y, int nvec, int precision, double shift,
                       bool allow_scratch = true);
+// ci_explicit.cu: sigma with the explicit matrix (FP64, interleaved vectors)
+pq_status ci_ham_spmv(pq_ci_handle *h, const void *X, void *Y, int nvp);
 // exact FP64 columns H[:, dets[c]] into column-major W (one species)
 pq_status ci_unit_columns(pq_ci_handle *h, const std::vector<int64_t> &dets, double *W);
 // ci_sigma32.cu

@@ -183,6 +183,48 @@ class POLYQUANT_DETSET:
         return out
 
     # ---- eigen-solver ----------------------------------------------------------
+    # ---- explicit Hamiltonian (create_ham, explicit_ham.cpp:51-84) -----------
+    def create_ham(self, screening_threshold: float = 0.0, use_for_sigma: bool = True) -> int:
+        """Build the sparse H on the device; FP64 sigma then multiplies with it. Returns stored entries."""
+        nnz = ctypes.c_int64()
+        check(_lib.load().pq_ci_ham_build(self._h, screening_threshold, 1 if use_for_sigma else 0,
+                                          ctypes.byref(nnz)), "pq_ci_ham_build")
+        return nnz.value
+
+    def ham_csr(self, upper: bool = True):
+        """(row_ptr, col, val) numpy arrays; upper=True is the reference's upper-triangle storage."""
+        L = _lib.load()
+        nnz = ctypes.c_int64()
+        check(L.pq_ci_ham_csr(self._h, 1 if upper else 0, ctypes.byref(nnz), None, None, None), "pq_ci_ham_csr")
+        rp = np.zeros(self.N_dets + 1, dtype=np.int64)
+        col = np.zeros(max(nnz.value, 1), dtype=np.int32)
+        val = np.zeros(max(nnz.value, 1), dtype=np.float64)
+        check(L.pq_ci_ham_csr(self._h, 1 if upper else 0, ctypes.byref(nnz), rp.ctypes.data, col.ctypes.data,
+                              val.ctypes.data), "pq_ci_ham_csr")
+        return rp, col[:nnz.value], val[:nnz.value]
+
+    # ---- properties of CI vectors (s2.cpp, rdm1.cpp) -------------------------
+    def s2(self, C) -> np.ndarray:
+        """<S^2> of each column of C (torch CUDA tensor (n_dets, k) or (n_dets,))."""
+        torch = _torch()
+        X = C.reshape(self.N_dets, -1).t().contiguous().to(torch.float64)
+        out = np.zeros(X.shape[0])
+        check(_lib.load().pq_ci_s2(self._h, ctypes.c_void_p(X.data_ptr()), self.N_dets, X.shape[0], out.ctypes.data),
+              "pq_ci_s2")
+        return out
+
+    def rdm1(self, c, spin: int = 0) -> np.ndarray:
+        """One-particle density matrix (n_orb x n_orb) of the state vector c and the given spin."""
+        torch = _torch()
+        x = c.reshape(-1).contiguous().to(torch.float64)
+        n = self._desc.n_orb[0]
+        out = np.zeros((n, n), order="F")
+        check(_lib.load().pq_ci_rdm1(self._h, ctypes.c_void_p(x.data_ptr()), spin, out.ctypes.data), "pq_ci_rdm1")
+        return out
+
+    def release_ham(self):
+        check(_lib.load().pq_ci_ham_release(self._h))
+
     def davidson(self, num_states: int = 1, num_subspace_vec: int = 5, iteration_max: int = 500,
                  convergence_E: float = 1e-6, precision: int = PQ_FP64, energy_shift: float = 0.0,
                  max_subspace: int = 0, return_vectors: bool = False, verbose: bool = False):

@@ -1,0 +1,122 @@
+"""<S^2> and the 1-RDM of CI vectors on the GPU (evaluate_s2, src/ci/detset/s2.cpp:4-123; create_1rdm,
+src/ci/detset/rdm1.cpp:4-72) against a direct numpy restatement of the same formulas."""
+import numpy as np
+import pytest
+
+import oracle as O
+from cases import batch_dict, h2o_problem, synthetic_fci
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def phase(m, h, p):
+    lo, hi = min(h, p), max(h, p)
+    return -1.0 if bin(m & (((1 << hi) - 1) ^ ((1 << (lo + 1)) - 1))).count("1") % 2 else 1.0
+
+
+def masks(d, sp):
+    return [int(w[-1]) if np.ndim(w) else int(w) for w in d.strings(0, sp)]
+
+
+def singles(masks_list):
+    out = {}
+    for i, m in enumerate(masks_list):
+        out[i] = [(j, n) for j, n in enumerate(masks_list) if bin(m ^ n).count("1") == 2]
+    return out
+
+
+def s2_numpy(d, C):
+    A, B = masks(d, 0), masks(d, 1)
+    u = d.unfold()
+    index = {(int(a), int(b)): k for k, (a, b) in enumerate(u)}
+    sa = singles(A)
+    res = np.zeros(C.shape[1])
+    for I, (ia, ib) in enumerate(u):
+        am, bm = A[ia], B[ib]
+        op = am ^ bm
+        n_open, n_a = bin(op).count("1"), bin(op & am).count("1")
+        sz = n_a - 0.5 * n_open
+        res += C[I] ** 2 * (n_a + sz * (sz - 1.0))
+        for ja, jam in sa[ia]:
+            ha = (am & ~jam).bit_length() - 1
+            pa = (jam & ~am).bit_length() - 1
+            if not (bm >> pa) & 1 or (bm >> ha) & 1:
+                continue
+            jbm = bm ^ (1 << pa) ^ (1 << ha)
+            if jbm not in B:
+                continue
+            J = index.get((ja, B.index(jbm)))
+            if J is None:
+                continue
+            ph = phase(am, ha, pa) * phase(bm, pa, ha)
+            res -= ph * C[I] * C[J]
+    return res
+
+
+def rdm1_numpy(d, c, spin, n):
+    S = masks(d, spin)
+    u = d.unfold()
+    index = {(int(a), int(b)): k for k, (a, b) in enumerate(u)}
+    ss = singles(S)
+    R = np.zeros((n, n))
+    for I, key in enumerate(u):
+        key = [int(x) for x in key]
+        m = S[key[spin]]
+        for o in range(n):
+            if (m >> o) & 1:
+                R[o, o] += c[I] ** 2
+        for js, jm in ss[key[spin]]:
+            kk = list(key)
+            kk[spin] = js
+            J = index.get(tuple(kk))
+            if J is None or J > I:
+                continue
+            k = (m & ~jm).bit_length() - 1
+            l = (jm & ~m).bit_length() - 1
+            v = phase(m, k, l) * c[I] * c[J]
+            R[k, l] += v
+            R[l, k] += v
+    return R
+
+
+@pytest.fixture(scope="module", params=["h2o_cisd", "fci_6o_3a2b", "fci_7o_3a3b"])
+def case(request, h2o):
+    from polyquant_gb300.detset import POLYQUANT_DETSET
+
+    p = {"h2o_cisd": lambda: h2o_problem(h2o("library"), [2, 2, 2]),
+         "fci_6o_3a2b": lambda: synthetic_fci(6, 3, 2, seed=2),
+         "fci_7o_3a3b": lambda: synthetic_fci(7, 3, 3, seed=3)}[request.param]()
+    d = O.Detset(p)
+    g = POLYQUANT_DETSET(**batch_dict(p))
+    w, V = np.linalg.eigh(d.dense_ham())
+    yield p, d, g, w, V
+    g.close()
+
+
+def test_s2_matches_restatement_and_is_a_spin_value(case):
+    p, d, g, w, V = case
+    X = V[:, :4]
+    s2 = g.s2(torch.from_numpy(X).cuda())
+    ref = s2_numpy(d, X)
+    assert np.abs(s2 - ref).max() < 1e-10
+    # eigenvectors of H are spin eigenstates: S(S+1) with S = |n_a - n_b|/2, +1, ...
+    S = np.sqrt(s2 + 0.25) - 0.5
+    assert np.abs(S - np.round(2 * S) / 2).max() < 1e-6
+    rng = np.random.default_rng(1)
+    Y = rng.standard_normal((d.n_dets, 9))
+    assert np.abs(g.s2(torch.from_numpy(Y).cuda()) - s2_numpy(d, Y)).max() < 1e-9 * np.abs(Y).max() ** 2 * d.n_dets
+
+
+def test_rdm1_matches_restatement(case):
+    p, d, g, w, V = case
+    n = p.n_orb[0]
+    c = V[:, 0]
+    for spin, ne in ((0, p.n_alpha[0]), (1, p.n_beta[0])):
+        R = g.rdm1(torch.from_numpy(c).cuda(), spin)
+        ref = rdm1_numpy(d, c, spin, n)
+        assert np.abs(R - ref).max() < 1e-12
+        assert abs(np.trace(R) - ne) < 1e-10
+        assert np.abs(R - R.T).max() < 1e-12
+        ev = np.linalg.eigvalsh(R)
+        assert ev.min() > -1e-10 and ev.max() < 1 + 1e-10
