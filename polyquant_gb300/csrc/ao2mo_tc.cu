@@ -347,18 +347,22 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 // ---------------------------------------------------------------------------
 // operand preparation
 template <bool TF32> struct Split;
+// The split works in FP32: hi + lo carry at most 2 x 8 (BF16) or 2 x 11
+// (TF32) significant bits, fewer than FP32's 24, and GB300 runs FP64
+// arithmetic at a small fraction of the FP32 rate (one FP64 -> FP32
+// conversion per element remains for FP64 sources).
 template <> struct Split<false> {
   using T = __nv_bfloat16;
-  static __device__ __forceinline__ void run(double x, T &h, T &l) {
-    h = __double2bfloat16(x);
-    l = __double2bfloat16(x - (double)__bfloat162float(h));
+  static __device__ __forceinline__ void run(float x, T &h, T &l) {
+    h = __float2bfloat16_rn(x);
+    l = __float2bfloat16_rn(x - __bfloat162float(h));
   }
 };
 template <> struct Split<true> {
   using T = float;
-  static __device__ __forceinline__ void run(double x, T &h, T &l) {
-    h = tf32_round((float)x);
-    l = tf32_round((float)(x - (double)h));
+  static __device__ __forceinline__ void run(float x, T &h, T &l) {
+    h = tf32_round(x);
+    l = tf32_round(x - h);
   }
 };
 
@@ -369,7 +373,7 @@ __global__ void split_ct_kernel(const double *C, int64_t ldc, int n_ao, int n_mo
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)n_mo * ld) return;
   int m = (int)(i / ld), mu = (int)(i - (int64_t)m * ld);
-  double x = mu < n_ao ? C[mu + (int64_t)m * ldc] : 0.0;
+  float x = mu < n_ao ? (float)C[mu + (int64_t)m * ldc] : 0.0f;
   Split<TF32>::run(x, hi[i], lo[i]);
 }
 
@@ -386,7 +390,7 @@ template <bool TF32>
 __global__ void __launch_bounds__(256) split_slices_kernel(const double *src64, const float *src32, int64_t ld, int n,
                                                            int ld_row, int64_t b0, typename Split<TF32>::T *hi,
                                                            typename Split<TF32>::T *lo) {
-  __shared__ double tile[32][33];
+  __shared__ float tile[32][33];
   const int nt = (n + 31) / 32;
   const int tv = blockIdx.y / nt, tm = blockIdx.y - tv * nt;
   if (tm > tv) return;
@@ -395,10 +399,10 @@ __global__ void __launch_bounds__(256) split_slices_kernel(const double *src64, 
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   for (int y = ty; y < 32; y += 8) {
     const int nu = tv * 32 + y, mu = tm * 32 + tx;
-    double x = 0.0;
+    float x = 0.0f;
     if (nu < n && mu <= nu) {
       const int64_t pr = (int64_t)nu * (nu + 1) / 2 + mu;
-      x = src64 ? src64[pr + c * ld] : (double)src32[c * ld + pr];
+      x = src64 ? (float)src64[pr + c * ld] : src32[c * ld + pr];
       Split<TF32>::run(x, H[(int64_t)nu * ld_row + mu], L[(int64_t)nu * ld_row + mu]);
     }
     tile[y][tx] = x;
