@@ -50,6 +50,7 @@ template <typename T> struct ProbT {
   const T *ps_h, *pd_h;            // positron single / double elements (signed, complete)
   const T *dpt;                    // [x][pair_e][Jp]: sum over occupied positron orbitals r of (pq|rr)
   const T *dea, *deb;              // [I][y][pair_p]: sum over occupied electron orbitals p of (pp|rs)
+  const T *mtab;                   // [x][pair_e][e]: sign_p(e) (pair_e | rs(e)) for positron single entry e
 };
 
 struct Prob {
@@ -59,7 +60,7 @@ struct Prob {
   const int32_t *ps_off, *ps_code, *pd_off, *pd_I;  // CSR over Jp
   const double *diag;
   int64_t n_dets;
-  int na, nb, npe, npp, P;
+  int na, nb, npe, npp, P, nps;  // nps: positron single entries over all Jp
   double cf;
   ProbT<float> f;
   ProbT<double> d;
@@ -223,20 +224,16 @@ __device__ void do_rows(const Prob &p, const Call &cl, const Unit &U, T *stg, in
             if (Ji >= 0) {
               const T sc = ngi ? -cf : cf;
               const T *dpt = q.dpt + ((int64_t)x * npe + phi) * P;
-              const T *epx0 = q.ep[x][0] + (int64_t)phi * npp, *epx1 = q.ep[x][1] + (int64_t)phi * npp;
+              const T *mt = q.mtab + ((int64_t)x * npe + phi) * p.nps;
 #pragma unroll
               for (int j = 0; j < J; j++) {
                 const int c = gl + j * G;
                 if (c >= L) continue;
                 const int Jp = c >> lw, v = c & ((1 << lw) - 1);
-                T s = (vi + sc * dpt[Jp]) * xv[j];
-                for (int e = p.ps_off[Jp]; e < p.ps_off[Jp + 1]; e++) {
-                  const int code = p.ps_code[e];
-                  const int Ip = code & 255, prs = code >> 10;
-                  const T ev = ((code >> 8) & 1) ? epx1[prs] : epx0[prs];
-                  s += (((code >> 9) & 1) ? -sc : sc) * ev * srow[(Ip << lw) + v];
-                }
-                acc[j] += s;
+                T s = vi * xv[j];
+                T t = dpt[Jp] * xv[j];
+                for (int e = p.ps_off[Jp]; e < p.ps_off[Jp + 1]; e++) t += mt[e] * srow[((p.ps_code[e] & 255) << lw) + v];
+                acc[j] += s + sc * t;
               }
             }
             __syncwarp();
@@ -419,19 +416,14 @@ __device__ void do_rows_lane(const Prob &p, const Call &cl, const Unit &U, T *st
             if (c < L) slot[c] = xv[c];
           }
           const T *dpt = q.dpt + ((int64_t)x * npe + ph) * P;
-          const T *epx0 = q.ep[x][0] + (int64_t)ph * npp, *epx1 = q.ep[x][1] + (int64_t)ph * npp;
+          const T *mt = q.mtab + ((int64_t)x * npe + ph) * p.nps;
 #pragma unroll
           for (int c = 0; c < LV; c++) {
             if (c >= L) continue;
             const int Jp = c >> lw, v = c & ((1 << lw) - 1);
-            T s = (val + sc * dpt[Jp]) * xv[c];
-            for (int e = p.ps_off[Jp]; e < p.ps_off[Jp + 1]; e++) {
-              const int code = p.ps_code[e];
-              const int Ip = code & 255, prs = code >> 10;
-              const T ev = ((code >> 8) & 1) ? epx1[prs] : epx0[prs];
-              s += (((code >> 9) & 1) ? -sc : sc) * ev * slot[(Ip << lw) + v];
-            }
-            acc[c] += s;
+            T t = dpt[Jp] * xv[c];
+            for (int e = p.ps_off[Jp]; e < p.ps_off[Jp + 1]; e++) t += mt[e] * slot[((p.ps_code[e] & 255) << lw) + v];
+            acc[c] += val * xv[c] + sc * t;
           }
         }
       }
@@ -575,7 +567,7 @@ using namespace pq::batch;
 // the problem's own handle.
 struct BatchTables {
   DevBuf ps_off, ps_code, pd_off, pd_I;
-  DevBuf ps_h64, ps_h32, pd_h64, pd_h32, dpt64, dpt32, dea64, dea32, deb64, deb32;
+  DevBuf ps_h64, ps_h32, pd_h64, pd_h32, dpt64, dpt32, dea64, dea32, deb64, deb32, mt64, mt32;
 };
 
 struct BatchPlan {
@@ -766,6 +758,16 @@ pq_status build_positron_tables(pq_ci_handle *h, BatchTables &bt, Prob &pr, cuda
     return t;
   };
   std::vector<double> dea = de_table(h->str[0][0], 0), deb = de_table(h->str[0][1], 1);
+  // electron-single x positron-single coefficients per (electron spin, electron pair, positron entry)
+  const int nps = (int)ps_code.size();
+  std::vector<double> mtab((size_t)2 * npe * std::max(nps, 1), 0.0);
+  for (int x = 0; x < 2; x++)
+    for (int pe = 0; pe < npe; pe++)
+      for (int e = 0; e < nps; e++) {
+        const int code = ps_code[e];
+        const double v = EP(x, (code >> 8) & 1, pe, code >> 10);
+        mtab[((size_t)x * npe + pe) * nps + e] = ((code >> 9) & 1) ? -v : v;
+      }
   if (ps_code.empty()) ps_code.push_back(0), ps_h.push_back(0.0);
   if (pd_I.empty()) pd_I.push_back(0), pd_h.push_back(0.0);
   PQ_TRY(upload(bt.ps_off, ps_off, st));
@@ -777,6 +779,7 @@ pq_status build_positron_tables(pq_ci_handle *h, BatchTables &bt, Prob &pr, cuda
   PQ_TRY(upload_pair(bt.dpt64, bt.dpt32, dpt, st));
   PQ_TRY(upload_pair(bt.dea64, bt.dea32, dea, st));
   PQ_TRY(upload_pair(bt.deb64, bt.deb32, deb, st));
+  PQ_TRY(upload_pair(bt.mt64, bt.mt32, mtab, st));
   PQ_CUDA_TRY(cudaStreamSynchronize(st));  // host vectors go out of scope
   pr.ps_off = bt.ps_off.as<int32_t>();
   pr.ps_code = bt.ps_code.as<int32_t>();
@@ -792,6 +795,9 @@ pq_status build_positron_tables(pq_ci_handle *h, BatchTables &bt, Prob &pr, cuda
   pr.f.dea = bt.dea32.as<float>();
   pr.d.deb = bt.deb64.as<double>();
   pr.f.deb = bt.deb32.as<float>();
+  pr.d.mtab = bt.mt64.as<double>();
+  pr.f.mtab = bt.mt32.as<float>();
+  pr.nps = nps;
   for (int x = 0; x < 2; x++)
     for (int y = 0; y < 2; y++) {
       pr.d.ep[x][y] = h->d_ep64[x][y].as<double>();
