@@ -33,25 +33,26 @@ template <bool FILL>
 __global__ void __launch_bounds__(128) ham_rows_kernel(ConnArgs a, int na, double thr, int32_t *cnt,
                                                        const int64_t *row_ptr, int32_t *col, double *val) {
   const int ia = blockIdx.x;
-  const int ib = blockIdx.y * blockDim.x + threadIdx.x;
-  if (ia >= na || ib >= a.rowlen[ia]) return;
-  const ConnRow r = conn_row(a, ia, ib);
-  const int64_t tot = r.total();
-  int64_t w = FILL ? row_ptr[r.I] : 0;
-  int32_t c = 0;
-  for (int64_t t = 0; t < tot; t++) {
-    double v;
-    const int64_t J = conn_elem(a, r, t, &v);
-    if (!keep_elem(J, r.I, v, thr)) continue;
-    if (FILL) {
-      col[w] = (int32_t)J;
-      val[w] = v;
-      w++;
-    } else {
-      c++;
+  if (ia >= na) return;
+  for (int ib = blockIdx.y * blockDim.x + threadIdx.x; ib < a.rowlen[ia]; ib += gridDim.y * blockDim.x) {
+    const ConnRow r = conn_row(a, ia, ib);
+    const int64_t tot = r.total();
+    int64_t w = FILL ? row_ptr[r.I] : 0;
+    int32_t c = 0;
+    for (int64_t t = 0; t < tot; t++) {
+      double v;
+      const int64_t J = conn_elem(a, r, t, &v);
+      if (!keep_elem(J, r.I, v, thr)) continue;
+      if (FILL) {
+        col[w] = (int32_t)J;
+        val[w] = v;
+        w++;
+      } else {
+        c++;
+      }
     }
+    if (!FILL) cnt[r.I] = c;
   }
-  if (!FILL) cnt[r.I] = c;
 }
 
 // Y[I][v] = sum_k val[k] X[col[k]][v], warp per row, interleaved vectors (nvp per det)
@@ -113,7 +114,7 @@ static pq_status ham_build(pq_ci_handle *h, double thr) {
   const ConnArgs a = make_conn_args(h);
   const int na = (int)h->rowlen.size();
   const int maxlen = *std::max_element(h->rowlen.begin(), h->rowlen.end());
-  const dim3 grid((unsigned)na, (unsigned)((maxlen + 127) / 128));
+  const dim3 grid((unsigned)na, (unsigned)std::min((maxlen + 127) / 128, 65535));
   DevBuf dcnt;
   PQ_TRY(dcnt.alloc(sizeof(int32_t) * (n + 1)));
   ham_rows_kernel<false><<<grid, 128, 0, st>>>(a, na, thr, dcnt.as<int32_t>(), nullptr, nullptr, nullptr);

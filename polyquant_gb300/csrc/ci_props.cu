@@ -26,11 +26,10 @@ __global__ void __launch_bounds__(PROP_THREADS) s2_kernel(ConnArgs a, int na, co
                                                           double *out) {
   __shared__ double red[S2_MAXV][PROP_THREADS / 32];
   const int ia = blockIdx.x;
-  const int ib = blockIdx.y * blockDim.x + threadIdx.x;
   double acc[S2_MAXV];
 #pragma unroll
   for (int v = 0; v < S2_MAXV; v++) acc[v] = 0.0;
-  if (ia < na && ib < a.rowlen[ia]) {
+  for (int ib = blockIdx.y * blockDim.x + threadIdx.x; ia < na && ib < a.rowlen[ia]; ib += gridDim.y * blockDim.x) {
     const ConnRow r = conn_row(a, ia, ib);
     double cI[S2_MAXV];
 #pragma unroll
@@ -40,7 +39,7 @@ __global__ void __launch_bounds__(PROP_THREADS) s2_kernel(ConnArgs a, int na, co
     const double sz = n_a - 0.5 * n_open;
     const double d = n_a + sz * (sz - 1.0);
 #pragma unroll
-    for (int v = 0; v < S2_MAXV; v++) acc[v] = cI[v] * cI[v] * d;
+    for (int v = 0; v < S2_MAXV; v++) acc[v] += cI[v] * cI[v] * d;
     for (int s = 0; s < r.n1a; s++) {
       const int Ja = a.a1_J[r.a1b + s], infa = a.a1_info[r.a1b + s];
       const uint64_t jam = a.astr[Ja];
@@ -83,8 +82,7 @@ __global__ void __launch_bounds__(PROP_THREADS) rdm1_kernel(ConnArgs a, int na, 
   for (int i = threadIdx.x; i < n * n; i += blockDim.x) acc[i] = 0.0;
   __syncthreads();
   const int ia = blockIdx.x;
-  const int ib = blockIdx.y * blockDim.x + threadIdx.x;
-  if (ia < na && ib < a.rowlen[ia]) {
+  for (int ib = blockIdx.y * blockDim.x + threadIdx.x; ia < na && ib < a.rowlen[ia]; ib += gridDim.y * blockDim.x) {
     const ConnRow r = conn_row(a, ia, ib);
     const double cI = C[r.I];
     const uint64_t mine = spin == 0 ? r.am : r.bm;
@@ -147,7 +145,7 @@ pq_status pq_ci_s2(pq_ci_handle *h, const double *C, int64_t ldc, int32_t nvec, 
   const ConnArgs a = make_conn_args(h);
   const int na = (int)h->rowlen.size();
   const int maxlen = *std::max_element(h->rowlen.begin(), h->rowlen.end());
-  const dim3 grid((unsigned)na, (unsigned)((maxlen + PROP_THREADS - 1) / PROP_THREADS));
+  const dim3 grid((unsigned)na, (unsigned)std::min((maxlen + PROP_THREADS - 1) / PROP_THREADS, 65535));
   DevBuf out;
   PQ_TRY(out.alloc(sizeof(double) * S2_MAXV));
   for (int v0 = 0; v0 < nvec; v0 += S2_MAXV) {
@@ -172,7 +170,7 @@ pq_status pq_ci_rdm1(pq_ci_handle *h, const double *C, int32_t spin, double *rdm
   const ConnArgs a = make_conn_args(h);
   const int na = (int)h->rowlen.size();
   const int maxlen = *std::max_element(h->rowlen.begin(), h->rowlen.end());
-  const dim3 grid((unsigned)na, (unsigned)((maxlen + PROP_THREADS - 1) / PROP_THREADS));
+  const dim3 grid((unsigned)na, (unsigned)std::min((maxlen + PROP_THREADS - 1) / PROP_THREADS, 65535));
   DevBuf out;
   PQ_TRY(out.alloc(sizeof(double) * n * n));
   PQ_CUDA_TRY(cudaMemsetAsync(out.ptr, 0, sizeof(double) * n * n, h->stream));
