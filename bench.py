@@ -116,6 +116,17 @@ def workload_name():
     return f"FCI {N_ORB} orbitals {N_A}a+{N_B}b, {nd:,} determinants, {ROOTS} roots, seed {SEED}"
 
 
+def max_over_ranks(x: float, dist=None, device: str = "cuda") -> float:
+    """The slowest rank's value (replicas run the same workload; the job takes as long as the slowest)."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.item()
+
+
 def cpu_baseline(C_host=None, budget_s=15.0, threads=None):
     """Time the oracle's gather sigma (the reference's element formulas, OpenMP) on a row sample."""
     import oracle as O
@@ -443,12 +454,7 @@ def main():
             sigma(prec)
         ev1.record()
         barrier()
-        ms = ev0.elapsed_time(ev1) / steps
-        if dist is not None:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = t.item()
-        return ms
+        return max_over_ranks(ev0.elapsed_time(ev1) / steps, dist)
 
     with ClockSampler(local) as clk:
         ms64 = timed(PQ_FP64, args.steps, args.warmup)

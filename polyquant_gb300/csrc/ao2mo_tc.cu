@@ -535,7 +535,7 @@ static pq_status ao2mo_tc_impl(const double *eri_ao, int layout, int64_t n, cons
   using E = typename tc::Split<TF32>::T;
   const int64_t npa = n * (n + 1) / 2, npm = nm * (nm + 1) / 2;
   const int ld = (int)((n + 7) / 8 * 8);    // AO row length (16-byte rows for TMA)
-  DevBuf full, cth, ctl, sh, sl, uh, ul, H1, H1t, Erow, err;
+  DevBuf full, cth, ctl, sh, sl, uh, ul, H1, H1t, err;
   const double *pairs = eri_ao;
   if (layout == PQ_AO_PACKED8) {
     PQ_TRY(full.alloc(sizeof(double) * npa * npa));
@@ -591,26 +591,35 @@ static pq_status ao2mo_tc_impl(const double *eri_ao, int layout, int64_t n, cons
   };
   // half 1 over AO ket pairs: H1[ket][ij]
   PQ_TRY(half(pairs, nullptr, npa, npa, H1.as<float>()));
-  full.release();
-  // H1t[ij][ket]
-  PQ_TRY(H1t.alloc(sizeof(float) * npa * npm));
+  // H1t[ij][ket], in the expanded pair matrix's memory when there is one (it is not read again):
+  // each reuse saves an allocation and a synchronising free inside the call
+  float *h1t = nullptr;
+  if (full.ptr && full.bytes >= sizeof(float) * npa * npm) {
+    h1t = full.as<float>();
+  } else {
+    PQ_TRY(H1t.alloc(sizeof(float) * npa * npm));
+    h1t = H1t.as<float>();
+  }
   {
     dim3 grid((unsigned)((npm + 31) / 32), (unsigned)((npa + 31) / 32));
     if (grid.y > 65535) {
       set_error("ao2mo: too many pairs for the transpose grid");
       return PQ_ERR_ARG;
     }
-    tc::transpose32_kernel<float><<<grid, dim3(32, 8), 0, st>>>(H1.as<float>(), npa, npm, H1t.as<float>());
+    tc::transpose32_kernel<float><<<grid, dim3(32, 8), 0, st>>>(H1.as<float>(), npa, npm, h1t);
     PQ_CUDA_TRY(cudaGetLastError());
   }
-  H1.release();
-  // half 2 over MO bra pairs: Erow[ij][kl]; slices read from rows of H1t (row ij holds the AO pair vector)
-  PQ_TRY(Erow.alloc(sizeof(float) * npm * npm));
-  PQ_TRY(half(nullptr, H1t.as<float>(), npa, npm, Erow.as<float>()));
-  H1t.release();
+  // half 2 over MO bra pairs: Erow[ij][kl], in H1's memory when it fits (npm <= npa); slices read from rows of H1t
+  DevBuf Erow;
+  float *erow = H1.as<float>();
+  if (npm > npa) {
+    PQ_TRY(Erow.alloc(sizeof(float) * npm * npm));
+    erow = Erow.as<float>();
+  }
+  PQ_TRY(half(nullptr, h1t, npa, npm, erow));
   {
     dim3 grid((unsigned)((npm + 31) / 32), (unsigned)((npm + 31) / 32));
-    tc::transpose32_kernel<double><<<grid, dim3(32, 8), 0, st>>>(Erow.as<float>(), npm, npm, eri_mo);
+    tc::transpose32_kernel<double><<<grid, dim3(32, 8), 0, st>>>(erow, npm, npm, eri_mo);
     PQ_CUDA_TRY(cudaGetLastError());
   }
   int herr = 0;
