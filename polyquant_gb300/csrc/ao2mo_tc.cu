@@ -310,26 +310,60 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 #pragma unroll
         for (int j = 0; j < 32; j++) stg[lane * EPI_LD + j] = v[j];
         __syncwarp();
-        const int n = c0 + lane;
-        for (int rr = 0; rr < 32; rr++) {
-          const int m = row0 + rr;
-          if (m >= g.M) break;
-          const float x = stg[rr * EPI_LD + lane];
-          if constexpr (EPI == EPI_SPLIT) {
-            if (n < g.N) {
-              const int64_t o = ((int64_t)b * g.M + m) * g.ld_out + n;
-              if constexpr (TF32) {
-                const float h = tf32_round(x);
-                static_cast<float *>(g.out_hi)[o] = h;
-                static_cast<float *>(g.out_lo)[o] = tf32_round(x - h);
+        if constexpr (EPI == EPI_SPLIT) {
+          // four lanes per row, eight consecutive columns per lane: 16-byte stores
+          // (rows of ld_out = a multiple of 8 elements, so n0 keeps them aligned)
+          const int cq = (lane & 3) * 8, n0 = c0 + cq;
+#pragma unroll
+          for (int it = 0; it < 4; it++) {
+            const int rr = it * 8 + (lane >> 2), m = row0 + rr;
+            if (m >= g.M || n0 >= g.N) continue;
+            float x[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) x[k] = stg[rr * EPI_LD + cq + k];
+            const int64_t o = ((int64_t)b * g.M + m) * g.ld_out + n0;
+            if constexpr (TF32) {
+              float h[8], l[8];
+#pragma unroll
+              for (int k = 0; k < 8; k++) {
+                h[k] = tf32_round(x[k]);
+                l[k] = tf32_round(x[k] - h[k]);
+              }
+              float *oh = static_cast<float *>(g.out_hi) + o, *ol = static_cast<float *>(g.out_lo) + o;
+              if (n0 + 8 <= g.N) {
+                reinterpret_cast<float4 *>(oh)[0] = make_float4(h[0], h[1], h[2], h[3]);
+                reinterpret_cast<float4 *>(oh)[1] = make_float4(h[4], h[5], h[6], h[7]);
+                reinterpret_cast<float4 *>(ol)[0] = make_float4(l[0], l[1], l[2], l[3]);
+                reinterpret_cast<float4 *>(ol)[1] = make_float4(l[4], l[5], l[6], l[7]);
               } else {
-                const __nv_bfloat16 h = __float2bfloat16_rn(x);
-                static_cast<__nv_bfloat16 *>(g.out_hi)[o] = h;
-                static_cast<__nv_bfloat16 *>(g.out_lo)[o] = __float2bfloat16_rn(x - __bfloat162float(h));
+                for (int k = 0; k < g.N - n0; k++) oh[k] = h[k], ol[k] = l[k];
+              }
+            } else {
+              __nv_bfloat162 h2[4], l2[4];
+#pragma unroll
+              for (int k = 0; k < 4; k++) {
+                h2[k] = __floats2bfloat162_rn(x[2 * k], x[2 * k + 1]);
+                l2[k] = __floats2bfloat162_rn(x[2 * k] - __low2float(h2[k]), x[2 * k + 1] - __high2float(h2[k]));
+              }
+              __nv_bfloat16 *oh = static_cast<__nv_bfloat16 *>(g.out_hi) + o;
+              __nv_bfloat16 *ol = static_cast<__nv_bfloat16 *>(g.out_lo) + o;
+              if (n0 + 8 <= g.N) {
+                *reinterpret_cast<uint4 *>(oh) = *reinterpret_cast<const uint4 *>(h2);
+                *reinterpret_cast<uint4 *>(ol) = *reinterpret_cast<const uint4 *>(l2);
+              } else {
+                const __nv_bfloat16 *hs = reinterpret_cast<const __nv_bfloat16 *>(h2);
+                const __nv_bfloat16 *ls = reinterpret_cast<const __nv_bfloat16 *>(l2);
+                for (int k = 0; k < g.N - n0; k++) oh[k] = hs[k], ol[k] = ls[k];
               }
             }
-          } else {
-            if (n <= m && n < g.N) g.out_pack[(int64_t)b * g.pack_stride + (int64_t)m * (m + 1) / 2 + n] = x;
+          }
+        } else {
+          const int n = c0 + lane;
+          for (int rr = 0; rr < 32; rr++) {
+            const int m = row0 + rr;
+            if (m >= g.M) break;
+            if (n <= m && n < g.N)
+              g.out_pack[(int64_t)b * g.pack_stride + (int64_t)m * (m + 1) / 2 + n] = stg[rr * EPI_LD + lane];
           }
         }
         __syncwarp();

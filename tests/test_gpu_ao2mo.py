@@ -52,7 +52,7 @@ def test_h2o_sto3galls_against_reference_fixture(h2o, golden):
 
 
 @pytest.mark.parametrize("mode", ["fp64", "bf16x3", "tf32x3"])
-@pytest.mark.parametrize("n,n_mo", [(24, 24), (40, 32), (64, 64), (136, 120)])
+@pytest.mark.parametrize("n,n_mo", [(24, 24), (30, 27), (40, 32), (64, 64), (136, 120)])
 def test_packed8_transform(mode, n, n_mo):
     from polyquant_gb300.integral import ao2mo
 
