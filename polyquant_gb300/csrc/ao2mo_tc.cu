@@ -416,10 +416,33 @@ __device__ __forceinline__ int64_t tri64(int64_t i, int64_t j) { return i > j ? 
 // slice b of a pair-matrix source, split: S[b][nu][mu] = src(tri(mu,nu), b0 + b)
 // src64: column-major (ld x ncols) FP64 pair matrix (element (r, c) at r + c*ld)
 // src32: row-major FP32 pair rows (element (r, c) at c*ld + r), i.e. row c holds the slice
+// Split two consecutive row elements (a at o, b at o + 1; o even, so the pair
+// is 4-byte (BF16) or 8-byte (TF32) aligned) into hi/lo with one vector store
+// each when both are wanted.
+template <bool TF32>
+__device__ __forceinline__ void split_store2(typename Split<TF32>::T *H, typename Split<TF32>::T *L, int64_t o, float a,
+                                             float b, bool va, bool vb) {
+  if (va && vb) {
+    if constexpr (TF32) {
+      const float ha = tf32_round(a), hb = tf32_round(b);
+      *reinterpret_cast<float2 *>(H + o) = make_float2(ha, hb);
+      *reinterpret_cast<float2 *>(L + o) = make_float2(tf32_round(a - ha), tf32_round(b - hb));
+    } else {
+      const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+      *reinterpret_cast<__nv_bfloat162 *>(H + o) = h;
+      *reinterpret_cast<__nv_bfloat162 *>(L + o) = __floats2bfloat162_rn(a - __low2float(h), b - __high2float(h));
+    }
+  } else {
+    if (va) Split<TF32>::run(a, H[o], L[o]);
+    if (vb) Split<TF32>::run(b, H[o + 1], L[o + 1]);
+  }
+}
+
 // One block per (slice, 32x32 tile of the lower triangle): the tile is read
 // with consecutive pair indices (mu <= nu) and written to both triangles, the
 // upper one through a shared-memory transpose, so loads and stores are
-// coalesced and every slice spreads over many SMs.
+// coalesced and every slice spreads over many SMs.  Each thread handles two
+// consecutive columns (16 column pairs x 16 rows per pass).
 template <bool TF32>
 __global__ void __launch_bounds__(256) split_slices_kernel(const double *src64, const float *src32, int64_t ld, int n,
                                                            int ld_row, int64_t b0, typename Split<TF32>::T *hi,
@@ -430,21 +453,23 @@ __global__ void __launch_bounds__(256) split_slices_kernel(const double *src64, 
   if (tm > tv) return;
   const int64_t b = blockIdx.x, c = b0 + b;
   typename Split<TF32>::T *H = hi + b * (int64_t)n * ld_row, *L = lo + b * (int64_t)n * ld_row;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  for (int y = ty; y < 32; y += 8) {
-    const int nu = tv * 32 + y, mu = tm * 32 + tx;
-    float x = 0.0f;
-    if (nu < n && mu <= nu) {
-      const int64_t pr = (int64_t)nu * (nu + 1) / 2 + mu;
-      x = src64 ? (float)src64[pr + c * ld] : src32[c * ld + pr];
-      Split<TF32>::run(x, H[(int64_t)nu * ld_row + mu], L[(int64_t)nu * ld_row + mu]);
-    }
-    tile[y][tx] = x;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  for (int y = ty; y < 32; y += 16) {
+    const int nu = tv * 32 + y, mu = tm * 32 + 2 * tx;
+    const bool va = nu < n && mu <= nu, vb = nu < n && mu + 1 <= nu;
+    float xa = 0.0f, xb = 0.0f;
+    const int64_t pr = (int64_t)nu * (nu + 1) / 2 + mu;
+    if (va) xa = src64 ? (float)src64[pr + c * ld] : src32[c * ld + pr];
+    if (vb) xb = src64 ? (float)src64[pr + 1 + c * ld] : src32[c * ld + pr + 1];
+    split_store2<TF32>(H, L, (int64_t)nu * ld_row + mu, xa, xb, va, vb);
+    tile[y][2 * tx] = xa;
+    tile[y][2 * tx + 1] = xb;
   }
   __syncthreads();
-  for (int y = ty; y < 32; y += 8) {
-    const int mu = tm * 32 + y, nu = tv * 32 + tx;
-    if (nu < n && mu < nu) Split<TF32>::run(tile[tx][y], H[(int64_t)mu * ld_row + nu], L[(int64_t)mu * ld_row + nu]);
+  for (int y = ty; y < 32; y += 16) {
+    const int row = tm * 32 + y, nu = tv * 32 + 2 * tx;
+    const bool va = nu < n && row < nu, vb = nu + 1 < n && row < nu + 1;
+    split_store2<TF32>(H, L, (int64_t)row * ld_row + nu, tile[2 * tx][y], tile[2 * tx + 1][y], va, vb);
   }
 }
 
