@@ -47,6 +47,14 @@ pq_status pq_ao2mo(const double *eri_ao, int32_t layout, int64_t n_ao_a, int64_t
 pq_status pq_mo1(const double *F_ao, int64_t n_ao, const double *C, int64_t ldc, int64_t n_mo, double *h_mo,
                  void *stream);
 
+/* Diagnostic hook, no reference counterpart: budget, in SM clock cycles, of
+ * the waits inside the tensor-core GEMM pipeline (<= 0 restores the default of
+ * about 2 s).  A wait that runs out makes the transform return PQ_TIMEOUT
+ * after the kernel has waited (with the default budget) for its own loads and
+ * MMAs and freed its tensor memory; the context stays usable.  Meant for
+ * tests of that path. */
+pq_status pq_debug_set_wait_budget(long long cycles);
+
 #ifdef __cplusplus
 }
 #endif

@@ -64,6 +64,7 @@ struct GemmArgs {
   void *out_hi, *out_lo;       // EPI_SPLIT outputs [b][M][ld_out]
   float *out_pack;             // EPI_PACK output [b][M(M+1)/2]
   int64_t pack_stride;         // elements per batch of out_pack
+  long long wait_cycles;       // budget of the pipeline waits (the wind-down waits keep WAIT_CYCLES)
   int *err;
 };
 
@@ -87,11 +88,11 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// bounded wait: true when the phase completed, false when the budget ran out
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// bounded wait: true when the phase completed, false when the budget (SM clock cycles) ran out
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long budget = WAIT_CYCLES) {
   const long long t0 = clock64();
   while (!mbar_try(bar, parity)) {
-    if (clock64() - t0 > WAIT_CYCLES) return false;
+    if (clock64() - t0 > budget) return false;
   }
   return true;
 }
@@ -223,7 +224,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       for (int s = 0; s < nst; s++, gs++) {
         const int slot = gs % STAGES;
         const uint32_t ph = (uint32_t)((gs / STAGES) & 1);
-        if (!mbar_wait(smem_u32(empty + slot), ph ^ 1u)) {
+        if (!mbar_wait(smem_u32(empty + slot), ph ^ 1u, g.wait_cycles)) {
           atomicCAS(g.err, 0, ERR_TIMEOUT_MMA);
           *abort_flag = 1;
           break;
@@ -249,7 +250,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     for (int t = blockIdx.x; t < n_tiles && !*abort_flag; t += gridDim.x, i++) {
       const int a = i & 1;
       const uint32_t aph = (uint32_t)((i >> 1) & 1);
-      if (!mbar_wait(smem_u32(acce + a), aph ^ 1u)) {
+      if (!mbar_wait(smem_u32(acce + a), aph ^ 1u, g.wait_cycles)) {
         atomicCAS(g.err, 0, ERR_TIMEOUT_ACC);
         *abort_flag = 1;
         break;
@@ -260,7 +261,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       for (int s = 0; s < nst; s++, gs++) {
         const int slot = gs % STAGES;
         const uint32_t ph = (uint32_t)((gs / STAGES) & 1);
-        if (!mbar_wait(smem_u32(full + slot), ph)) {
+        if (!mbar_wait(smem_u32(full + slot), ph, g.wait_cycles)) {
           atomicCAS(g.err, 0, ERR_TIMEOUT_FULL);
           *abort_flag = 1;
           ok = false;
@@ -294,7 +295,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, i++) {
       const int a = i & 1;
       const uint32_t aph = (uint32_t)((i >> 1) & 1);
-      const bool ok = mbar_wait(smem_u32(accf + a), aph);
+      const bool ok = mbar_wait(smem_u32(accf + a), aph, g.wait_cycles);
       if (!ok || *abort_flag) {
         if (!ok && lane == 0) atomicCAS(g.err, 0, ERR_TIMEOUT_ACC);
         *abort_flag = 1;
@@ -516,6 +517,9 @@ __global__ void transpose32_kernel(const float *in, int64_t rows, int64_t cols, 
 }  // namespace tc
 
 // ---------------------------------------------------------------------------
+// budget of the GEMM pipeline waits; pq_debug_set_wait_budget changes it for tests of the timeout path
+static long long g_gemm_wait_cycles = tc::WAIT_CYCLES;
+
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   if (!fn) {
@@ -576,6 +580,7 @@ static pq_status run_gemm(const Operand &A, const Operand &B, bool a_batched, bo
   g.a_rows = M;
   g.b_rows = N;
   g.nbatch = nbatch;
+  g.wait_cycles = g_gemm_wait_cycles;
   auto kern = tc::tc_gemm_kernel<TF32, EPI>;
   PQ_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES));
   int dev = 0, sms = 0;
@@ -702,3 +707,8 @@ pq_status ao2mo_tc(const double *eri_ao, int layout, int64_t n_ao, const double 
 }
 
 }  // namespace pq
+
+extern "C" pq_status pq_debug_set_wait_budget(long long cycles) {
+  pq::g_gemm_wait_cycles = cycles > 0 ? cycles : pq::tc::WAIT_CYCLES;
+  return PQ_OK;
+}

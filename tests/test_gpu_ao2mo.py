@@ -111,3 +111,24 @@ def test_mo_one_body():
     h = calculate_mo_1_body_integrals(torch.from_numpy(F).cuda(), torch.from_numpy(C).cuda(), 1, 2).cpu().numpy()
     Cs = C[:, 1:10]
     assert np.abs(h - Cs.T @ F @ Cs).max() < 1e-12
+
+
+def test_gemm_wait_timeout_returns_status_and_context_survives():
+    """Bounded waits of the tensor-core GEMM: with a one-cycle pipeline budget every CTA gives up at its first
+    pending wait, waits (with the default budget) for its own loads and MMAs, frees TMEM and returns; the call
+    reports PQ_TIMEOUT and the next call on the same context is correct."""
+    from polyquant_gb300._lib import PQ_TIMEOUT, PQError, load
+    from polyquant_gb300.integral import ao2mo
+
+    packed, C, ref = _packed_case(64, n_mo=64, seed=5)
+    P, Cd = torch.from_numpy(packed).cuda(), torch.from_numpy(C).cuda()
+    L = load()
+    L.pq_debug_set_wait_budget(1)
+    try:
+        with pytest.raises(PQError) as e:
+            ao2mo(P, Cd, mode=_modes()["bf16x3"])
+        assert e.value.status == PQ_TIMEOUT
+    finally:
+        L.pq_debug_set_wait_budget(0)
+    out = ao2mo(P, Cd, mode=_modes()["bf16x3"]).cpu().numpy()
+    assert np.abs(out - ref).max() / np.abs(ref).max() < TOL["bf16x3"]
