@@ -186,3 +186,19 @@ def test_invalid_problem_is_an_error():
     p = synthetic_fci(5, 3, 3, seed=0, ex=[3, 3, 6])
     with pytest.raises(PQError):
         gpu_detset(p)
+
+
+def test_davidson_iteration_cap_reports_not_converged():
+    """An iteration cap that is too small ends the solve with PQ_NOT_CONVERGED (the reference aborts,
+    epci.cpp:620) and still returns the current Ritz values and residual."""
+    from polyquant_gb300._lib import PQ_FP32, PQ_FP64
+
+    p = synthetic_fci(8, 4, 4, seed=1)
+    ds = gpu_detset(p)
+    w = np.linalg.eigvalsh(O.Detset(p).dense_ham())
+    for prec in (PQ_FP64, PQ_FP32):
+        e, info = ds.davidson(num_states=2, num_subspace_vec=4, convergence_E=1e-10, iteration_max=3, precision=prec)
+        assert not info["converged"]
+        assert info["iterations"] == 3 and info["max_residual"] > 1e-10
+        assert np.all(e >= w[:2] - 1e-9)  # Ritz values bound the eigenvalues from above
+    ds.close()
