@@ -498,7 +498,7 @@ __device__ __forceinline__ void do_unit(const Prob &p, const Call &cl, const Uni
   }
 }
 
-__global__ void __launch_bounds__(256) batch_sigma_kernel(const Prob *__restrict__ probs,
+__global__ void __launch_bounds__(256, 3) batch_sigma_kernel(const Prob *__restrict__ probs,
                                                           const Call *__restrict__ calls,
                                                           const Unit *__restrict__ units, int n_units,
                                                           unsigned *counter) {
