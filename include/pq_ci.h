@@ -174,16 +174,17 @@ pq_status pq_ci_ham_release(pq_ci_handle *h);
  * query *nnz first. */
 pq_status pq_ci_ham_csr(pq_ci_handle *h, int32_t upper, int64_t *nnz, int64_t *row_ptr, int32_t *col, double *val);
 
-/* ---- properties of CI vectors (one species) --------------------------------
- * <S^2> of nvec states: replaces POLYQUANT_DETSET::evaluate_s2
- * (src/ci/detset/s2.cpp:4-123).  C: DEVICE, n_dets x nvec column-major;
- * s2: host, nvec values. */
+/* ---- properties of CI vectors ----------------------------------------------
+ * <S^2> of nvec states for every species: replaces
+ * POLYQUANT_DETSET::evaluate_s2 (src/ci/detset/s2.cpp:4-123).  C: DEVICE,
+ * n_dets x nvec column-major; s2: host, nvec x n_species values, state-major
+ * (s2[v * n_species + s]). */
 pq_status pq_ci_s2(pq_ci_handle *h, const double *C, int64_t ldc, int32_t nvec, double *s2);
 
-/* One-particle density matrix of one state and spin (0 alpha, 1 beta):
- * replaces create_1rdm (src/ci/detset/rdm1.cpp:4-72).  C: DEVICE, n_dets
- * values; rdm: host, n_orb x n_orb column-major. */
-pq_status pq_ci_rdm1(pq_ci_handle *h, const double *C, int32_t spin, double *rdm);
+/* One-particle density matrix of one state, species and spin (0 alpha,
+ * 1 beta): replaces create_1rdm (src/ci/detset/rdm1.cpp:4-72).  C: DEVICE,
+ * n_dets values; rdm: host, n_orb[species] x n_orb[species] column-major. */
+pq_status pq_ci_rdm1(pq_ci_handle *h, const double *C, int32_t species, int32_t spin, double *rdm);
 
 /* ---- batches of independent problems -------------------------------------
  * Many small CI problems of uneven size solved together: one persistent sigma

@@ -116,7 +116,7 @@ def load(path: str = LIB_PATH):
     L.pq_ci_s2.restype = I32
     L.pq_ci_s2.argtypes = [P, P, I64, I32, P]
     L.pq_ci_rdm1.restype = I32
-    L.pq_ci_rdm1.argtypes = [P, P, I32, P]
+    L.pq_ci_rdm1.argtypes = [P, P, I32, I32, P]
     L.pq_ci_batch_create.restype = I32
     L.pq_ci_batch_create.argtypes = [ctypes.POINTER(PQDesc), I32, P, ctypes.POINTER(P)]
     L.pq_ci_batch_destroy.restype = I32

@@ -140,7 +140,7 @@ def run(kw: CIKeywords, problem: Optional[dict] = None, e_const: float = 0.0) ->
             out["method"] = "davidson"
             out["report"] = info
         out["energies"] = (np.asarray(e) + e_const).tolist()
-        if kw.calc_s2 and ds.n_species == 1:
+        if kw.calc_s2:
             out["s2"] = ds.s2(vecs).tolist()
     finally:
         ds.close()

@@ -205,21 +205,23 @@ class POLYQUANT_DETSET:
 
     # ---- properties of CI vectors (s2.cpp, rdm1.cpp) -------------------------
     def s2(self, C) -> np.ndarray:
-        """<S^2> of each column of C (torch CUDA tensor (n_dets, k) or (n_dets,))."""
+        """<S^2> of each column of C (torch CUDA tensor (n_dets, k) or (n_dets,)): shape (k,) for one species,
+        (k, n_species) for two."""
         torch = _torch()
         X = C.reshape(self.N_dets, -1).t().contiguous().to(torch.float64)
-        out = np.zeros(X.shape[0])
+        out = np.zeros((X.shape[0], self.n_species))
         check(_lib.load().pq_ci_s2(self._h, ctypes.c_void_p(X.data_ptr()), self.N_dets, X.shape[0], out.ctypes.data),
               "pq_ci_s2")
-        return out
+        return out[:, 0] if self.n_species == 1 else out
 
-    def rdm1(self, c, spin: int = 0) -> np.ndarray:
-        """One-particle density matrix (n_orb x n_orb) of the state vector c and the given spin."""
+    def rdm1(self, c, spin: int = 0, species: int = 0) -> np.ndarray:
+        """One-particle density matrix (n_orb x n_orb) of the state vector c for one species and spin."""
         torch = _torch()
         x = c.reshape(-1).contiguous().to(torch.float64)
-        n = self._desc.n_orb[0]
+        n = self._desc.n_orb[species]
         out = np.zeros((n, n), order="F")
-        check(_lib.load().pq_ci_rdm1(self._h, ctypes.c_void_p(x.data_ptr()), spin, out.ctypes.data), "pq_ci_rdm1")
+        check(_lib.load().pq_ci_rdm1(self._h, ctypes.c_void_p(x.data_ptr()), species, spin, out.ctypes.data),
+              "pq_ci_rdm1")
         return out
 
     def release_ham(self):

@@ -120,3 +120,87 @@ def test_rdm1_matches_restatement(case):
         assert np.abs(R - R.T).max() < 1e-12
         ev = np.linalg.eigvalsh(R)
         assert ev.min() > -1e-10 and ev.max() < 1 + 1e-10
+
+
+# ---- two species (electron + positron product space) -----------------------
+def s2_numpy_two(d, C, sp):
+    S = [[[int(w[-1]) for w in d.strings(s, x)] for x in (0, 1)] for s in (0, 1)]
+    u = [tuple(int(v) for v in row) for row in d.unfold()]
+    index = {key: k for k, key in enumerate(u)}
+    res = np.zeros(C.shape[1])
+    for I, key in enumerate(u):
+        am, bm = S[sp][0][key[2 * sp]], S[sp][1][key[2 * sp + 1]]
+        op = am ^ bm
+        n_open, n_a = bin(op).count("1"), bin(op & am).count("1")
+        sz = n_a - 0.5 * n_open
+        res += C[I] ** 2 * (n_a + sz * (sz - 1.0))
+        for ja, jam in enumerate(S[sp][0]):
+            if bin(am ^ jam).count("1") != 2:
+                continue
+            ha = (am & ~jam).bit_length() - 1
+            pa = (jam & ~am).bit_length() - 1
+            if not (bm >> pa) & 1 or (bm >> ha) & 1:
+                continue
+            jbm = bm ^ (1 << pa) ^ (1 << ha)
+            if jbm not in S[sp][1]:
+                continue
+            kk = list(key)
+            kk[2 * sp], kk[2 * sp + 1] = ja, S[sp][1].index(jbm)
+            J = index.get(tuple(kk))
+            if J is None:
+                continue
+            res -= phase(am, ha, pa) * phase(bm, pa, ha) * C[I] * C[J]
+    return res
+
+
+def rdm1_numpy_two(d, c, sp, spin, n):
+    S = [int(w[-1]) for w in d.strings(sp, spin)]
+    u = [tuple(int(v) for v in row) for row in d.unfold()]
+    index = {key: k for k, key in enumerate(u)}
+    R = np.zeros((n, n))
+    slot = 2 * sp + spin
+    for I, key in enumerate(u):
+        m = S[key[slot]]
+        for o in range(n):
+            if (m >> o) & 1:
+                R[o, o] += c[I] ** 2
+        for js, jm in enumerate(S):
+            if bin(m ^ jm).count("1") != 2:
+                continue
+            kk = list(key)
+            kk[slot] = js
+            J = index.get(tuple(kk))
+            if J is None or J > I:
+                continue
+            k = (m & ~jm).bit_length() - 1
+            l = (jm & ~m).bit_length() - 1
+            v = phase(m, k, l) * c[I] * c[J]
+            R[k, l] += v
+            R[l, k] += v
+    return R
+
+
+@pytest.mark.parametrize("args", [(5, 2, 2, 4, 1, 1, 3), (6, 2, 1, 5, 1, 0, 4)])
+def test_two_species_s2_and_rdm1(args):
+    from cases import synthetic_ep
+    from polyquant_gb300.detset import POLYQUANT_DETSET
+
+    ne, ea, eb, npo, pa, pb, seed = args
+    p = synthetic_ep(ne, ea, eb, npo, pa, pb, seed=seed)
+    d = O.Detset(p)
+    g = POLYQUANT_DETSET(**batch_dict(p))
+    w, V = np.linalg.eigh(d.dense_ham())
+    X = V[:, :3]
+    s2 = g.s2(torch.from_numpy(X).cuda())
+    assert s2.shape == (3, 2)
+    for sp in (0, 1):
+        assert np.abs(s2[:, sp] - s2_numpy_two(d, X, sp)).max() < 1e-10
+        S = np.sqrt(s2[:, sp] + 0.25) - 0.5
+        assert np.abs(S - np.round(2 * S) / 2).max() < 1e-6
+    c = V[:, 0]
+    for sp, nelec in ((0, (ea, eb)), (1, (pa, pb))):
+        for spin in (0, 1):
+            R = g.rdm1(torch.from_numpy(c).cuda(), spin=spin, species=sp)
+            assert np.abs(R - rdm1_numpy_two(d, c, sp, spin, p.n_orb[sp])).max() < 1e-12
+            assert abs(np.trace(R) - nelec[spin]) < 1e-10
+    g.close()

@@ -39,7 +39,7 @@ int use_all(void) {
   st |= pq_ci_ham_csr(h, 1, &nnz, NULL, NULL, NULL);
   st |= pq_ci_ham_release(h);
   st |= pq_ci_s2(h, NULL, n, 1, s2);
-  st |= pq_ci_rdm1(h, NULL, 0, NULL);
+  st |= pq_ci_rdm1(h, NULL, 0, 0, NULL);
   st |= pq_ci_destroy(h);
   st |= pq_ci_batch_create(&d, 1, NULL, &b);
   st |= pq_ci_batch_num_dets(b, 0, &n);
