@@ -157,9 +157,11 @@ pq_status pq_ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *e
 
 /* ---- explicit sparse Hamiltonian ------------------------------------------
  * Replaces POLYQUANT_DETSET::create_ham (src/ci/detset/explicit_ham.cpp:51-84,
- * explicit_ham_singleparticle.cpp; the reference's default build_matrix path)
- * and its use through Spectra::SparseSymMatProd (src/ci/epci.cpp:623-668).
- * Builds H on the device (one species, FP64); exact zeros are dropped and,
+ * explicit_ham_singleparticle.cpp, explicit_ham_mixedparticle.cpp; the
+ * reference's default build_matrix path) and its use through
+ * Spectra::SparseSymMatProd (src/ci/epci.cpp:623-668).  Builds H on the device
+ * (one species or an electron-positron product space, FP64); exact zeros are
+ * dropped and,
  * for screening_threshold > 0, every |H_IJ| <= threshold (the reference's
  * ham.prune(threshold, 1.0)).  use_for_sigma != 0 makes FP64 sigma calls
  * (pq_ci_sigma*, pq_ci_davidson's FP64 requests) multiply with the matrix;

@@ -120,11 +120,11 @@ def run(kw: CIKeywords, problem: Optional[dict] = None, e_const: float = 0.0) ->
     k = min(kw.num_states, ds.N_dets)
     out = {"n_dets": ds.N_dets, "method": None}
     try:
-        if kw.build_matrix and ds.n_species == 1:
+        if kw.build_matrix:
             out["nnz"] = ds.create_ham(screening_threshold=kw.screening_threshold, use_for_sigma=True)
         if kw.exact_diag:
-            if not (kw.build_matrix and ds.n_species == 1):
-                raise ValueError("exact_diag needs build_matrix and one species")
+            if not kw.build_matrix:
+                raise ValueError("exact_diag needs build_matrix")
             rp, col, val = ds.ham_csr(upper=False)
             H = np.zeros((ds.N_dets, ds.N_dets))
             for i in range(ds.N_dets):

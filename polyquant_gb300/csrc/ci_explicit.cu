@@ -13,7 +13,9 @@
 // enumerator (ci_conn.cuh).  sigma with the explicit matrix is a warp-per-row
 // gather over the interleaved vectors.  pq_ci_ham_csr exports the reference's
 // layout (upper triangle with the diagonal, columns ascending) or the full
-// matrix.  One species; FP64.
+// matrix.  FP64.  A two-species (electron-positron) space uses the same
+// count/fill passes over the product-space enumerator of ci_two.cu
+// (two_species_create_ham, explicit_ham_mixedparticle.cpp:190-553).
 #include <algorithm>
 #include <numeric>
 
@@ -101,24 +103,25 @@ pq_status ci_ham_spmv(pq_ci_handle *h, const void *X, void *Y, int nvp) {
 }
 
 static pq_status ham_build(pq_ci_handle *h, double thr) {
-  if (h->n_species != 1) {
-    set_error("pq_ci_ham_build: the explicit Hamiltonian is built for one species");
-    return PQ_ERR_ARG;
-  }
   if (h->n_dets > 0x7fffffffLL) {
     set_error("pq_ci_ham_build: %lld determinants exceed 32-bit column indices", (long long)h->n_dets);
     return PQ_ERR_ARG;
   }
   const int64_t n = h->n_dets;
   cudaStream_t st = h->stream;
-  const ConnArgs a = make_conn_args(h);
+  const bool two = h->n_species == 2;
+  const ConnArgs a = two ? ConnArgs{} : make_conn_args(h);
   const int na = (int)h->rowlen.size();
   const int maxlen = *std::max_element(h->rowlen.begin(), h->rowlen.end());
   const dim3 grid((unsigned)na, (unsigned)std::min((maxlen + 127) / 128, 65535));
   DevBuf dcnt;
   PQ_TRY(dcnt.alloc(sizeof(int32_t) * (n + 1)));
-  ham_rows_kernel<false><<<grid, 128, 0, st>>>(a, na, thr, dcnt.as<int32_t>(), nullptr, nullptr, nullptr);
-  PQ_CUDA_TRY(cudaGetLastError());
+  if (two) {
+    PQ_TRY(ci_ham_rows2(h, thr, dcnt.as<int32_t>(), nullptr, nullptr, nullptr));
+  } else {
+    ham_rows_kernel<false><<<grid, 128, 0, st>>>(a, na, thr, dcnt.as<int32_t>(), nullptr, nullptr, nullptr);
+    PQ_CUDA_TRY(cudaGetLastError());
+  }
   std::vector<int32_t> cnt(n);
   PQ_CUDA_TRY(cudaMemcpyAsync(cnt.data(), dcnt.ptr, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
   PQ_CUDA_TRY(cudaStreamSynchronize(st));
@@ -128,9 +131,13 @@ static pq_status ham_build(pq_ci_handle *h, double thr) {
   PQ_TRY(upload(h->d_hrow, rp, st));
   PQ_TRY(h->d_hcol.alloc(sizeof(int32_t) * (nnz + 1)));
   PQ_TRY(h->d_hval.alloc(sizeof(double) * (nnz + 1)));
-  ham_rows_kernel<true><<<grid, 128, 0, st>>>(a, na, thr, nullptr, h->d_hrow.as<int64_t>(), h->d_hcol.as<int32_t>(),
-                                              h->d_hval.as<double>());
-  PQ_CUDA_TRY(cudaGetLastError());
+  if (two) {
+    PQ_TRY(ci_ham_rows2(h, thr, nullptr, h->d_hrow.as<int64_t>(), h->d_hcol.as<int32_t>(), h->d_hval.as<double>()));
+  } else {
+    ham_rows_kernel<true><<<grid, 128, 0, st>>>(a, na, thr, nullptr, h->d_hrow.as<int64_t>(),
+                                                h->d_hcol.as<int32_t>(), h->d_hval.as<double>());
+    PQ_CUDA_TRY(cudaGetLastError());
+  }
   PQ_CUDA_TRY(cudaStreamSynchronize(st));
   h->h_nnz = nnz;
   return PQ_OK;

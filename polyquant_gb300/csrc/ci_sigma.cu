@@ -349,8 +349,8 @@ static pq_status sigma_dispatch(pq_ci_handle *h, const T *X, T *Y, double shift)
 
 pq_status ci_sigma_il(pq_ci_handle *h, const void *X, void *Y, int nvp, int precision, double shift,
                       bool allow_scratch) {
-  if (h->n_species == 2) return ci_sigma2_il(h, X, Y, nvp, precision, shift);
   if (h->use_explicit && precision == PQ_FP64 && shift == 0.0) return ci_ham_spmv(h, X, Y, nvp);
+  if (h->n_species == 2) return ci_sigma2_il(h, X, Y, nvp, precision, shift);
   if (precision == PQ_FP32 && allow_scratch && h->fp32_v2) return ci_sigma32_v2(h, X, Y, nvp, shift);
   if (precision == PQ_FP64) {
     if (nvp == 1) return sigma_dispatch<double, 1>(h, (const double *)X, (double *)Y, shift);

@@ -96,6 +96,75 @@ template <typename T> __device__ __forceinline__ T coul_col(const T *M, int ld, 
   return s;
 }
 
+// Every off-diagonal connection of determinant t (string indices per slot,
+// strings m) in the classes of the reference's singleshot builder: singles of
+// each of the four spin lists with their same-species and cross-species
+// Coulomb terms, alpha-beta doubles within a species, single x single cross
+// doubles, same-spin doubles.  f(J, H_IJ) is called for each partner J that is
+// in the determinant list; each partner appears once.
+template <typename T, typename F>
+__device__ __forceinline__ void two_conn_visit(const Args2<T> &p, const int (&t)[4], const uint64_t (&m)[4], F &&f) {
+  for (int s = 0; s < 4; s++) {
+    const int sp = s >> 1, spin = s & 1, other = s ^ 1;
+    const List2<T> &ls = p.l[s];
+    const int np = p.npair[sp];
+    const int64_t o0 = ls.s1_off[t[s]], o1 = ls.s1_off[t[s] + 1];
+    for (int64_t e = o0; e < o1; e++) {
+      const int info = __ldg(ls.s1_info + e);
+      const int pr = info >> 1;
+      const uint32_t neg = (uint32_t)(info & 1);
+      int tj[4] = {t[0], t[1], t[2], t[3]};
+      tj[s] = __ldg(ls.s1_J + e);
+      // single in slot s
+      const int64_t j = lookup2(p, tj);
+      if (j >= 0) {
+        T h = __ldg(ls.s1_F + e);
+        h += spin == 0 ? coul_row(p.eab[sp], np, pr, m[other]) : coul_col(p.eab[sp], np, pr, m[other]);
+        T x = 0;
+        if (sp == 0) {
+          x += coul_row(p.ep[p.blk[0][spin]][p.blk[1][0]], p.npair[1], pr, m[2]);
+          x += coul_row(p.ep[p.blk[0][spin]][p.blk[1][1]], p.npair[1], pr, m[3]);
+        } else {
+          x += coul_col(p.ep[p.blk[0][0]][p.blk[1][spin]], p.npair[1], pr, m[0]);
+          x += coul_col(p.ep[p.blk[0][1]][p.blk[1][spin]], p.npair[1], pr, m[1]);
+        }
+        h += p.cf * x;
+        if (neg) h = -h;
+        f(j, h);
+      }
+      // single x single in a later slot r
+      for (int r = s + 1; r < 4; r++) {
+        const List2<T> &lr = p.l[r];
+        const int64_t q0 = lr.s1_off[t[r]], q1 = lr.s1_off[t[r] + 1];
+        for (int64_t g = q0; g < q1; g++) {
+          int tk[4] = {tj[0], tj[1], tj[2], tj[3]};
+          tk[r] = __ldg(lr.s1_J + g);
+          const int64_t k = lookup2(p, tk);
+          if (k < 0) continue;
+          const int info2 = __ldg(lr.s1_info + g);
+          const int pr2 = info2 >> 1;
+          T c;
+          if ((r >> 1) == sp) {  // alpha-beta double within one species
+            c = __ldg(p.eab[sp] + (int64_t)pr * np + pr2);
+          } else {                // cross-species double: species-0 slot s, species-1 slot r
+            c = p.cf * __ldg(p.ep[p.blk[0][spin]][p.blk[1][r & 1]] + (int64_t)pr * p.npair[1] + pr2);
+          }
+          if (neg ^ (uint32_t)(info2 & 1)) c = -c;
+          f(k, c);
+        }
+      }
+    }
+    // same-spin doubles in slot s
+    const int64_t d0 = ls.s2_off[t[s]], d1 = ls.s2_off[t[s] + 1];
+    for (int64_t e = d0; e < d1; e++) {
+      int tj[4] = {t[0], t[1], t[2], t[3]};
+      tj[s] = __ldg(ls.s2_J + e);
+      const int64_t j = lookup2(p, tj);
+      if (j >= 0) f(j, __ldg(ls.s2_D + e));
+    }
+  }
+}
+
 template <typename T, int NV>
 __global__ void __launch_bounds__(128) sigma_two_species_kernel(Args2<T> p) {
   const int ie = blockIdx.x;
@@ -112,68 +181,46 @@ __global__ void __launch_bounds__(128) sigma_two_species_kernel(Args2<T> p) {
     const T dI = (T)(p.diag[I] - p.shift);
 #pragma unroll
     for (int v = 0; v < NV; v++) acc[v] = dI * __ldg(p.X + I * NV + v);
-
-    for (int s = 0; s < 4; s++) {
-      const int sp = s >> 1, spin = s & 1, other = s ^ 1;
-      const List2<T> &ls = p.l[s];
-      const int np = p.npair[sp];
-      const int64_t o0 = ls.s1_off[t[s]], o1 = ls.s1_off[t[s] + 1];
-      for (int64_t e = o0; e < o1; e++) {
-        const int info = __ldg(ls.s1_info + e);
-        const int pr = info >> 1;
-        const uint32_t neg = (uint32_t)(info & 1);
-        int tj[4] = {t[0], t[1], t[2], t[3]};
-        tj[s] = __ldg(ls.s1_J + e);
-        // single in slot s
-        const int64_t j = lookup2(p, tj);
-        if (j >= 0) {
-          T h = __ldg(ls.s1_F + e);
-          h += spin == 0 ? coul_row(p.eab[sp], np, pr, m[other]) : coul_col(p.eab[sp], np, pr, m[other]);
-          T x = 0;
-          if (sp == 0) {
-            x += coul_row(p.ep[p.blk[0][spin]][p.blk[1][0]], p.npair[1], pr, m[2]);
-            x += coul_row(p.ep[p.blk[0][spin]][p.blk[1][1]], p.npair[1], pr, m[3]);
-          } else {
-            x += coul_col(p.ep[p.blk[0][0]][p.blk[1][spin]], p.npair[1], pr, m[0]);
-            x += coul_col(p.ep[p.blk[0][1]][p.blk[1][spin]], p.npair[1], pr, m[1]);
-          }
-          h += p.cf * x;
-          if (neg) h = -h;
-          axpy_gather<T, NV>(acc, h, p.X, j);
-        }
-        // single x single in a later slot r
-        for (int r = s + 1; r < 4; r++) {
-          const List2<T> &lr = p.l[r];
-          const int64_t q0 = lr.s1_off[t[r]], q1 = lr.s1_off[t[r] + 1];
-          for (int64_t f = q0; f < q1; f++) {
-            int tk[4] = {tj[0], tj[1], tj[2], tj[3]};
-            tk[r] = __ldg(lr.s1_J + f);
-            const int64_t k = lookup2(p, tk);
-            if (k < 0) continue;
-            const int info2 = __ldg(lr.s1_info + f);
-            const int pr2 = info2 >> 1;
-            T c;
-            if ((r >> 1) == sp) {  // alpha-beta double within one species
-              c = __ldg(p.eab[sp] + (int64_t)pr * np + pr2);
-            } else {                // cross-species double: species-0 slot s, species-1 slot r
-              c = p.cf * __ldg(p.ep[p.blk[0][spin]][p.blk[1][r & 1]] + (int64_t)pr * p.npair[1] + pr2);
-            }
-            if (neg ^ (uint32_t)(info2 & 1)) c = -c;
-            axpy_gather<T, NV>(acc, c, p.X, k);
-          }
-        }
-      }
-      // same-spin doubles in slot s
-      const int64_t d0 = ls.s2_off[t[s]], d1 = ls.s2_off[t[s] + 1];
-      for (int64_t e = d0; e < d1; e++) {
-        int tj[4] = {t[0], t[1], t[2], t[3]};
-        tj[s] = __ldg(ls.s2_J + e);
-        const int64_t j = lookup2(p, tj);
-        if (j >= 0) axpy_gather<T, NV>(acc, __ldg(ls.s2_D + e), p.X, j);
-      }
-    }
+    two_conn_visit(p, t, m, [&](int64_t j, T h) { axpy_gather<T, NV>(acc, h, p.X, j); });
 #pragma unroll
     for (int v = 0; v < NV; v++) p.Y[I * NV + v] = acc[v];
+  }
+}
+
+// Rows of the explicit Hamiltonian (two_species_create_ham,
+// explicit_ham_mixedparticle.cpp:190-553): the diagonal, then every kept
+// off-diagonal element; exact zeros are dropped and |H_IJ| <= thr pruned when
+// thr > 0, as ham.prune(thr, 1.0) does (explicit_ham.cpp:79-81).  FILL = false
+// counts the kept elements of each row, FILL = true writes them at row_ptr.
+template <bool FILL>
+__global__ void __launch_bounds__(128) ham_rows_two_kernel(Args2<double> p, double thr, int32_t *cnt,
+                                                           const int64_t *row_ptr, int32_t *col, double *val) {
+  const int ie = blockIdx.x;
+  const int L = p.elev[ie];
+  if (L < 0) return;
+  const int64_t nq = p.psize[L];
+  for (int64_t q = threadIdx.x; q < nq; q += blockDim.x) {
+    const int64_t I = p.ebase[ie] + q;
+    const int t[4] = {p.e_a[ie], p.e_b[ie], p.pdet_a[p.pfirst[L] + q], p.pdet_b[p.pfirst[L] + q]};
+    uint64_t m[4];
+#pragma unroll
+    for (int s = 0; s < 4; s++) m[s] = p.l[s].str[t[s]];
+    int64_t w = FILL ? row_ptr[I] : 0;
+    int32_t c = 0;
+    auto emit = [&](int64_t j, double h) {
+      const bool keep = thr > 0.0 ? fabs(h) > thr : (j == I || h != 0.0);
+      if (!keep) return;
+      if (FILL) {
+        col[w] = (int32_t)j;
+        val[w] = h;
+        w++;
+      } else {
+        c++;
+      }
+    };
+    emit(I, p.diag[I]);
+    two_conn_visit(p, t, m, emit);
+    if (!FILL) cnt[I] = c;
   }
 }
 
@@ -431,6 +478,17 @@ pq_status ci_sigma2_il(pq_ci_handle *h, const void *X, void *Y, int nvp, int pre
   }
   set_error("unsupported interleave width %d / precision %d", nvp, precision);
   return PQ_ERR_ARG;
+}
+
+pq_status ci_ham_rows2(pq_ci_handle *h, double thr, int32_t *cnt, const int64_t *row_ptr, int32_t *col, double *val) {
+  const Args2<double> a = make_args<double>(h);
+  const unsigned ne = (unsigned)h->e_a.size();
+  if (cnt)
+    ham_rows_two_kernel<false><<<ne, 128, 0, h->stream>>>(a, thr, cnt, nullptr, nullptr, nullptr);
+  else
+    ham_rows_two_kernel<true><<<ne, 128, 0, h->stream>>>(a, thr, nullptr, row_ptr, col, val);
+  PQ_CUDA_TRY(cudaGetLastError());
+  return PQ_OK;
 }
 
 pq_status ci_unfold2(const pq_ci_handle *h, int32_t *out) {

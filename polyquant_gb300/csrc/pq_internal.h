@@ -127,6 +127,8 @@ pq_status build_spin_tables(pq_ci_handle *h, int s, int sp, const double *h1_hos
 pq_status ci_build2(pq_ci_handle *h);
 pq_status ci_sigma2_il(pq_ci_handle *h, const void *X, void *Y, int nvp, int precision, double shift);
 pq_status ci_unfold2(const pq_ci_handle *h, int32_t *out);
+// explicit-H rows of a two-species space: counts when cnt != NULL, else fills col/val at row_ptr
+pq_status ci_ham_rows2(pq_ci_handle *h, double thr, int32_t *cnt, const int64_t *row_ptr, int32_t *col, double *val);
 // ci_sigma.cu
 // allow_scratch = false keeps sigma on kernels that need no work memory beyond X and Y
 pq_status ci_sigma_il(pq_ci_handle *h, const void *X, void *Y, int nvec, int precision, double shift,

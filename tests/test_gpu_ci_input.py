@@ -33,3 +33,19 @@ def test_cisd_from_json_and_fcidump(integrals, extra):
     assert out["n_dets"] == 141
     assert np.abs(np.array(out["energies"]) - E_CISD).max() < 1e-6
     assert abs(out["s2"][0]) < 1e-6  # closed-shell ground state: a singlet
+
+
+@pytest.mark.parametrize("extra", [{"build_matrix": True}, {"build_matrix": True, "exact_diag": True},
+                                   {"build_matrix": False}])
+def test_electron_positron_from_json(extra):
+    import oracle as O
+    from cases import synthetic_ep
+
+    p = synthetic_ep(5, 2, 2, 4, 1, 0, seed=7)
+    w = np.linalg.eigvalsh(O.Detset(p).dense_ham())
+    ck = {"convergence_E": 1e-9, "num_states": 2, "num_subspace_vec": 6, "calc_s2": True}
+    ck.update(extra)
+    out = ci_input.run(ci_input.parse({"keywords": {"ci_keywords": ck}}), problem=batch_dict(p), e_const=0.5)
+    assert ("nnz" in out) == extra["build_matrix"]
+    assert np.abs(np.array(out["energies"]) - 0.5 - w[:2]).max() < 1e-8
+    assert np.array(out["s2"]).shape == (2, 2)

@@ -1,9 +1,10 @@
-"""Explicit sparse Hamiltonian (create_ham, src/ci/detset/explicit_ham.cpp:51-84) against the oracle's dense H."""
+"""Explicit sparse Hamiltonian (create_ham, src/ci/detset/explicit_ham.cpp:51-84; one species
+explicit_ham_singleparticle.cpp, electron + positron explicit_ham_mixedparticle.cpp) against the oracle's dense H."""
 import numpy as np
 import pytest
 
 import oracle as O
-from cases import batch_dict, h2o_problem, synthetic_fci, synthetic_unrestricted
+from cases import batch_dict, h2o_problem, synthetic_ep, synthetic_fci, synthetic_unrestricted
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -13,6 +14,9 @@ CASES = {
     "h2o_fci": lambda h2o: h2o_problem(h2o("library"), [2, 2, 4]),
     "fci_8o_4a3b": lambda h2o: synthetic_fci(8, 4, 3, seed=5),
     "unrestricted_7o_3a2b": lambda h2o: synthetic_unrestricted(7, 3, 2, seed=1),
+    # electron + positron: CIS x CIS, and the full product under a collective excitation limit
+    "ep_cis": lambda h2o: synthetic_ep(6, 2, 1, 5, 1, 0, seed=2, ex_e=[1, 1, 1], ex_p=[1, 1, 1]),
+    "ep_coll3_2pos": lambda h2o: synthetic_ep(5, 2, 2, 4, 1, 1, seed=4, max_coll=3),
 }
 
 
@@ -82,14 +86,3 @@ def test_sigma_and_davidson_with_explicit_matrix(case):
     assert info["converged"]
     assert np.abs(e - w[:k]).max() < 1e-9
     g.release_ham()
-
-
-def test_two_species_rejected():
-    from polyquant_gb300.detset import POLYQUANT_DETSET
-    from polyquant_gb300._lib import PQError
-    from cases import synthetic_ep
-
-    g = POLYQUANT_DETSET(**batch_dict(synthetic_ep(4, 1, 1, 3, 1, 0, seed=1)))
-    with pytest.raises(PQError, match="one species"):
-        g.create_ham()
-    g.close()
