@@ -89,6 +89,8 @@ def lib():
             f.argtypes = [P, P, I64, ctypes.c_int, P, I64, ctypes.c_int]
         L.orc_sigma_rows.argtypes = [P, P, I64, ctypes.c_int, P, I64, P, ctypes.c_int]
         L.orc_dense_ham.argtypes = [P, P, ctypes.c_int]
+        L.orc_evaluate_s2.argtypes = [P, P, I64, ctypes.c_int, P, ctypes.c_int]
+        L.orc_create_1rdm.argtypes = [P, P, ctypes.c_int, ctypes.c_int, P, ctypes.c_int]
         L.orc_single_spin_num_excitation.restype = ctypes.c_int
         L.orc_single_spin_num_excitation.argtypes = [P, P, ctypes.c_int]
         L.orc_get_holes.restype = ctypes.c_int
@@ -306,6 +308,21 @@ class Detset:
         f = lib().orc_sigma_slow if slow else lib().orc_sigma_singleshot
         f(self._h, _ptr(C), self.n_dets, C.shape[1], _ptr(S), self.n_dets, nthreads)
         return S
+
+    def evaluate_s2(self, C: np.ndarray, nthreads: int = 0) -> np.ndarray:
+        """<S^2> of each column of C per species (s2.cpp:4-123): shape (k, n_species)."""
+        C = np.asfortranarray(np.asarray(C, dtype=np.float64).reshape(self.n_dets, -1))
+        out = np.zeros((C.shape[1], self.prob.n_species), order="F")
+        lib().orc_evaluate_s2(self._h, _ptr(C), self.n_dets, C.shape[1], _ptr(out), nthreads)
+        return out
+
+    def create_1rdm(self, c: np.ndarray, species: int = 0, spin: int = 0, nthreads: int = 0) -> np.ndarray:
+        """One-particle density matrix of one state (rdm1.cpp:4-72): n_orb x n_orb."""
+        c = np.ascontiguousarray(np.asarray(c, dtype=np.float64).reshape(-1))
+        n = self.prob.n_orb[species]
+        out = np.zeros((n, n), order="F")
+        lib().orc_create_1rdm(self._h, _ptr(c), species, spin, _ptr(out), nthreads)
+        return out
 
     def sigma_rows(self, C: np.ndarray, rows, nthreads: int = 0) -> np.ndarray:
         C = np.asfortranarray(np.asarray(C, dtype=np.float64).reshape(self.n_dets, -1))

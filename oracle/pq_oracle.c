@@ -1051,3 +1051,126 @@ void orc_sigma_rows(orc_detset *ds, const double *C, int64_t ldc, int nvec, cons
     for (int v = 0; v < nvec; v++) S_rows[r + v * n_rows] = acc[v];
   }
 }
+
+/* ------------------------------------------------------------------------- */
+/* s2.cpp:4-123 (evaluate_s2).  Per determinant and species: the diagonal
+ * n_a + s_z (s_z - 1) over the open shells, then every alpha single x beta
+ * single partner whose hole of one spin is the particle of the other
+ * subtracts phase_a * phase_b * C_I * C_J.  S2 is nvec x n_species,
+ * column-major. */
+void orc_evaluate_s2(const orc_detset *ds, const double *C, int64_t ldc, int nvec, double *S2, int nthreads) {
+  const int nsp = ds->d.n_species, nw = ds->n_words, ntup = ds->ntup;
+  const int nt = get_threads(nthreads);
+  double *part = (double *)calloc((size_t)nt * nvec * nsp, sizeof(double));
+#pragma omp parallel num_threads(nt)
+  {
+#ifdef _OPENMP
+    double *acc = part + (size_t)omp_get_thread_num() * nvec * nsp;
+#else
+    double *acc = part;
+#endif
+    int ha[64 * MAXW], pa[64 * MAXW], hb[64 * MAXW], pb[64 * MAXW];
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t i = 0; i < ds->n_dets; i++) {
+      const int32_t *iu = ds->unfold + i * ntup;
+      for (int v = 0; v < nvec; v++) {
+        const double ci = C[i + v * ldc];
+        if (ci == 0.0) continue;
+        for (int p = 0; p < nsp; p++) {
+          const int32_t ia = iu[2 * p], ib = iu[2 * p + 1];
+          const uint64_t *Da = getdet(ds, p, 0, ia), *Db = getdet(ds, p, 1, ib);
+          int n_tot = 0, n_a = 0;
+          for (int w = 0; w < nw; w++) {
+            const uint64_t x = Da[w] ^ Db[w];
+            n_tot += __builtin_popcountll(x);
+            n_a += __builtin_popcountll(x & Da[w]);
+          }
+          const double sz = n_a - 0.5 * n_tot;
+          acc[v + p * nvec] += ci * ci * (n_a + sz * (sz - 1.0));
+          const int32_t *la, *lb;
+          const int64_t na = orc_singles(ds, p, 0, ia, &la), nb = orc_singles(ds, p, 1, ib, &lb);
+          for (int64_t x = 0; x < na; x++)
+            for (int64_t y = 0; y < nb; y++) {
+              int32_t t[4] = {iu[0], iu[1], ntup > 2 ? iu[2] : 0, ntup > 2 ? iu[3] : 0};
+              t[2 * p] = la[x];
+              t[2 * p + 1] = lb[y];
+              const int64_t j = orc_lookup(ds, t);
+              if (j < 0) continue;
+              const double cj = C[j + v * ldc];
+              if (cj == 0.0) continue;
+              const uint64_t *Ja = getdet(ds, p, 0, la[x]), *Jb = getdet(ds, p, 1, lb[y]);
+              orc_get_holes(Da, Ja, nw, ha);
+              orc_get_parts(Da, Ja, nw, pa);
+              orc_get_holes(Db, Jb, nw, hb);
+              orc_get_parts(Db, Jb, nw, pb);
+              if (ha[0] == pb[0] && hb[0] == pa[0]) {
+                const double ph = orc_get_phase(Da, Ja, nw, ha, pa, 1) * orc_get_phase(Db, Jb, nw, hb, pb, 1);
+                acc[v + p * nvec] -= ph * ci * cj;
+              }
+            }
+        }
+      }
+    }
+  }
+  for (int k = 0; k < nvec * nsp; k++) {
+    double s = 0.0;
+    for (int t = 0; t < nt; t++) s += part[(size_t)t * nvec * nsp + k];
+    S2[k] = s;
+  }
+  free(part);
+}
+
+/* rdm1.cpp:4-72 (create_1rdm) for one species and spin: C_I^2 on the diagonal
+ * of each occupied orbital, and for each single partner J < I the product
+ * phase C_I C_J added at (hole, particle) and (particle, hole); contributions
+ * with magnitude <= 1e-16 are skipped.  All orbitals are taken as one irrep
+ * (the reference's symmetry-label filter admits every pair without point-group
+ * symmetry).  rdm is n_orb x n_orb, column-major. */
+void orc_create_1rdm(const orc_detset *ds, const double *c, int part, int spin, double *rdm, int nthreads) {
+  const int n = ds->d.n_orb[part], nw = ds->n_words, ntup = ds->ntup, slot = 2 * part + spin;
+  const double thresh = 1e-16;
+  const int nt = get_threads(nthreads);
+  double *acc_all = (double *)calloc((size_t)nt * n * n, sizeof(double));
+#pragma omp parallel num_threads(nt)
+  {
+#ifdef _OPENMP
+    double *acc = acc_all + (size_t)omp_get_thread_num() * n * n;
+#else
+    double *acc = acc_all;
+#endif
+    int occ[64 * MAXW], virt[64 * MAXW], h[64 * MAXW], q[64 * MAXW];
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t i = 0; i < ds->n_dets; i++) {
+      const int32_t *iu = ds->unfold + i * ntup;
+      const int32_t si = iu[slot];
+      const uint64_t *Di = getdet(ds, part, spin, si);
+      int no = 0, nv = 0;
+      orc_get_occ_virt(Di, nw, n, occ, &no, virt, &nv);
+      const double d = c[i] * c[i];
+      if (fabs(d) > thresh)
+        for (int k = 0; k < no; k++) acc[occ[k] + (int64_t)occ[k] * n] += d;
+      const int32_t *ls;
+      const int64_t ns = orc_singles(ds, part, spin, si, &ls);
+      for (int64_t x = 0; x < ns; x++) {
+        int32_t t[4] = {iu[0], iu[1], ntup > 2 ? iu[2] : 0, ntup > 2 ? iu[3] : 0};
+        t[slot] = ls[x];
+        const int64_t j = orc_lookup(ds, t);
+        if (j < 0 || i < j) continue;
+        const uint64_t *Dj = getdet(ds, part, spin, ls[x]);
+        orc_get_holes(Di, Dj, nw, h);
+        orc_get_parts(Di, Dj, nw, q);
+        const double v = orc_get_phase(Di, Dj, nw, h, q, 1) * c[i] * c[j];
+        if (fabs(v) > thresh) {
+          acc[h[0] + (int64_t)q[0] * n] += v;
+          acc[q[0] + (int64_t)h[0] * n] += v;
+        }
+      }
+    }
+  }
+  for (int64_t k = 0; k < (int64_t)n * n; k++) {
+    double s = 0.0;
+    for (int t = 0; t < nt; t++) s += acc_all[(size_t)t * n * n + k];
+    rdm[k] = s;
+  }
+  free(acc_all);
+}

@@ -69,6 +69,12 @@ void orc_sigma_rows(orc_detset *ds, const double *C, int64_t ldc, int nvec, cons
 /* explicit dense H (n_dets x n_dets, col-major), small cases only */
 void orc_dense_ham(orc_detset *ds, double *H, int nthreads);
 
+/* ---- properties of CI vectors (s2.cpp, rdm1.cpp) ---- */
+/* <S^2> per vector and species: S2 is nvec x n_species, col-major */
+void orc_evaluate_s2(const orc_detset *ds, const double *C, int64_t ldc, int nvec, double *S2, int nthreads);
+/* one-particle density matrix of one species and spin: n_orb x n_orb, col-major */
+void orc_create_1rdm(const orc_detset *ds, const double *c, int part, int spin, double *rdm, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif
