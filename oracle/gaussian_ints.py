@@ -189,8 +189,9 @@ def _eri_prim(pa: Prim, pb: Prim, pc: Prim, pd: Prim):
 class Molecule:
     """Atoms (symbol, position in bohr) ordered like the reference's AO list."""
 
-    def __init__(self, symbols, geometry_angstrom, basis: str = "file"):
-        table = BASES[basis]
+    def __init__(self, symbols, geometry_angstrom, basis="file"):
+        """``basis``: a name of BASES, or a table {symbol: [(kind, exponents, coefficients), ...]}."""
+        table = BASES[basis] if isinstance(basis, str) else basis
         geo = np.asarray(geometry_angstrom, float).reshape(-1, 3) / BOHR_TO_ANGSTROM
         atoms = list(zip(symbols, geo))
         order = sorted(range(len(atoms)), key=lambda k: (atoms[k][0], k))

@@ -98,6 +98,11 @@ class POLYQUANT_DETSET:
         check(L.pq_ci_num_dets(self._h, ctypes.byref(n)))
         self.N_dets = n.value
         self.n_species = ns
+        self.n_orb = [int(d.n_orb[s]) for s in range(ns)]
+        self.n_alpha = [int(d.n_alpha[s]) for s in range(ns)]
+        self.n_beta = [int(d.n_beta[s]) for s in range(ns)]
+        self.restricted = [int(d.restricted[s]) for s in range(ns)]
+        self.excitation_level = [[int(x) for x in d.ex_level[s]] for s in range(ns)]
         self._diag = None
 
     # ---- lifetime ---------------------------------------------------------

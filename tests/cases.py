@@ -53,3 +53,23 @@ def batch_dict(p):
     """CIProblem -> keyword dict of CIBatch / POLYQUANT_DETSET."""
     return dict(n_orb=p.n_orb, n_alpha=p.n_alpha, n_beta=p.n_beta, h1=p.h1, eri=p.eri, excitation_level=p.ex_level,
                 restricted=p.restricted, charge=p.charge, max_collective_excitation_level=p.max_collective)
+
+
+def h_minus():
+    """H- in the reference's five-shell s basis (golden fixture h_minus_no_golden.npz): AO integrals and RHF
+    from the oracle's Gaussian-integral code, MO integrals, and the CISD [1,1,2] problem of
+    tests/data/PsH_wpos/H_minus.json."""
+    import os
+
+    import gaussian_ints as G
+
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "h_minus_no_golden.npz"))
+    shells = [("s", list(g["shell_exp"][i, :n]), list(g["shell_coef"][i, :n])) for i, n in enumerate(g["shell_nprim"])]
+    mol = G.Molecule(["H"], [0.0, 0.0, 0.0], {"H": shells})
+    S, T, V = mol.one_body()
+    eri = mol.eri()
+    E, C, eps = G.rhf(S, T + V, eri, 1, mol.e_nuc())
+    h = C.T @ (T + V) @ C
+    p = O.CIProblem([C.shape[1]], [1], [1], [[h, h]], {(0, 0, 0, 0): O.ao2mo_full(eri, C, C)}, [[1, 1, 2]],
+                    restricted=[1], charge=[-1.0], e_const=mol.e_nuc())
+    return dict(problem=p, C=C, S=S, E_rhf=E, no_occ=g["no_occ"], no_ao=g["no_ao"])

@@ -1,32 +1,73 @@
-"""Regenerate tests/golden/h2o_sto3g_golden.npz from the reference's own fixtures.
+"""Regenerate the golden fixtures of tests/golden/ from the reference's own test data.
 
 Run once in a checkout that has the polyquant sources at $POLYQUANT_REF
-(default /root/reference); the npz is committed so that the tests never read
-the reference tree at run time.
+(default /root/reference); the npz files are committed so that the tests never
+read the reference tree at run time.
 
 Sources (paths inside the polyquant project):
-  tests/data/h2o_sto3glibrary_cisd/cisd_ham_elements.txt  141x141 CISD H, column 0
-      (compared in tests/integration_tests/calculation/calculation_test.cpp:253-307)
-  tests/data/h2o_sto3glibrary_cisd/ref_mo_onebody.txt      5x5 h_MO, sto3galls basis
-  tests/data/h2o_sto3glibrary_cisd/ref_eri.txt             (ij|kl) i<=j, k<=l, same basis
-      (both compared in tests/unit_tests/ci/ci_test.cpp:12-70)
+  h2o_sto3g_golden.npz
+    tests/data/h2o_sto3glibrary_cisd/cisd_ham_elements.txt  141x141 CISD H, column 0
+        (compared in tests/integration_tests/calculation/calculation_test.cpp:253-307)
+    tests/data/h2o_sto3glibrary_cisd/ref_mo_onebody.txt      5x5 h_MO, sto3galls basis
+    tests/data/h2o_sto3glibrary_cisd/ref_eri.txt             (ij|kl) i<=j, k<=l, same basis
+        (both compared in tests/unit_tests/ci/ci_test.cpp:12-70)
+  h_minus_no_golden.npz
+    tests/data/PsH_wpos/electron_basis.g94   the s basis of H- (five contracted shells)
+    tests/data/PsH_wpos/h_minus_NO_occ.txt   natural-orbital occupations (spin-summed)
+    tests/data/PsH_wpos/h_minus_NO.txt       natural orbitals in the AO basis
+        (compared in tests/unit_tests/ci/ci_test.cpp:854-871, "CI: Natural Orbitals";
+         input tests/data/PsH_wpos/H_minus.json: RHF, CISD [1,1,2], state 0)
 """
 import os
 
 import numpy as np
 
 REF = os.environ.get("POLYQUANT_REF", "/root/reference")
-D = os.path.join(REF, "tests", "data", "h2o_sto3glibrary_cisd")
+HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def main():
-    ham = np.loadtxt(os.path.join(D, "cisd_ham_elements.txt"))[:, 0].reshape(141, 141)
-    h1 = np.loadtxt(os.path.join(D, "ref_mo_onebody.txt"))
-    eri = np.loadtxt(os.path.join(D, "ref_eri.txt"))
-    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "h2o_sto3g_golden.npz")
+def read_g94_s_shells(path):
+    """(exponents, coefficients) of each shell of a Gaussian-94 basis file; s shells only."""
+    shells = []
+    lines = [ln.split() for ln in open(path) if ln.strip() and not ln.startswith("*")]
+    k = 1  # skip the element line
+    while k < len(lines):
+        kind, nprim = lines[k][0].lower(), int(lines[k][1])
+        if kind != "s":
+            raise ValueError(f"{path}: only s shells are read, found {kind}")
+        prims = [(float(a), float(c)) for a, c in (lines[k + 1 + i][:2] for i in range(nprim))]
+        shells.append(prims)
+        k += 1 + nprim
+    return shells
+
+
+def h2o():
+    d = os.path.join(REF, "tests", "data", "h2o_sto3glibrary_cisd")
+    ham = np.loadtxt(os.path.join(d, "cisd_ham_elements.txt"))[:, 0].reshape(141, 141)
+    h1 = np.loadtxt(os.path.join(d, "ref_mo_onebody.txt"))
+    eri = np.loadtxt(os.path.join(d, "ref_eri.txt"))
+    out = os.path.join(HERE, "h2o_sto3g_golden.npz")
     np.savez_compressed(out, cisd_ham=ham, alls_h1=h1, alls_eri=eri)
     print("wrote", out)
 
 
+def h_minus():
+    d = os.path.join(REF, "tests", "data", "PsH_wpos")
+    shells = read_g94_s_shells(os.path.join(d, "electron_basis.g94"))
+    mp = max(len(s) for s in shells)
+    exps = np.zeros((len(shells), mp))
+    coefs = np.zeros((len(shells), mp))
+    nprim = np.array([len(s) for s in shells], dtype=np.int32)
+    for i, s in enumerate(shells):
+        for j, (a, c) in enumerate(s):
+            exps[i, j], coefs[i, j] = a, c
+    occ = np.loadtxt(os.path.join(d, "h_minus_NO_occ.txt"))
+    no = np.loadtxt(os.path.join(d, "h_minus_NO.txt"))
+    out = os.path.join(HERE, "h_minus_no_golden.npz")
+    np.savez_compressed(out, shell_exp=exps, shell_coef=coefs, shell_nprim=nprim, no_occ=occ, no_ao=no)
+    print("wrote", out)
+
+
 if __name__ == "__main__":
-    main()
+    h2o()
+    h_minus()
