@@ -5,14 +5,17 @@ with the keys, value forms and defaults of the reference
 (src/calculation/calculation.cpp:274-389; defaults src/ci/epci.hpp:113-122,
 src/ci/determinant_set.hpp:195-196), plus three keys of this implementation:
 ``precision`` ("fp64" or "mixed"), ``batch`` and ``autotune``.  Keys the
-GB300 path does not implement (spin penalties, natural orbitals, printing
-thresholds) are collected in ``CIKeywords.unsupported`` instead of being
+GB300 path does not implement (spin penalties, symmetrised natural orbitals,
+printing thresholds) are collected in ``CIKeywords.unsupported`` instead of being
 silently dropped.
 
 ``run`` solves one CI problem as ``POLYQUANT_EPCI::run`` would
 (src/ci/epci.cpp:575-686): the explicit sparse Hamiltonian when
 ``build_matrix`` is set (the reference default), dense diagonalisation for
-``exact_diag``, block Davidson otherwise, and <S^2> per state for ``calc_s2``.
+``exact_diag``, block Davidson otherwise, <S^2> per state and species for
+``calc_s2``, and the natural spin orbitals of the ``NO_states`` (default
+[0]; calculate_NOs, epci.cpp:200-318) in the basis of the caller's SCF
+orbitals, or in the MO basis when none are given.
 The integrals come from the caller or from the FCIDUMP file named by
 ``fcidump_filename``.
 """
@@ -28,7 +31,8 @@ from .detset import INT_MAX
 
 SUPPORTED = {"convergence_E", "num_states", "num_subspace_vec", "iteration_max", "build_matrix", "exact_diag",
              "slow_diag", "excitation_level", "max_collective_excitation_level", "screening_threshold",
-             "frozen_core", "deleted_virtual", "calc_s2", "fcidump_filename", "precision", "batch", "autotune"}
+             "frozen_core", "deleted_virtual", "calc_s2", "NO_states", "fcidump_filename", "precision", "batch",
+             "autotune"}
 
 
 @dataclass
@@ -46,6 +50,7 @@ class CIKeywords:
     frozen_core: List[int] = field(default_factory=list)
     deleted_virtual: List[int] = field(default_factory=list)
     calc_s2: bool = False
+    NO_states: List[int] = field(default_factory=lambda: [0])
     fcidump_filename: Optional[str] = None
     precision: str = "fp64"
     batch: bool = False
@@ -79,7 +84,9 @@ def parse(data: Union[dict, str]) -> CIKeywords:
         if k not in SUPPORTED:
             kw.unsupported.append(k)
             continue
-        if k in ("frozen_core", "deleted_virtual"):
+        if k == "NO_states":
+            v = [int(x) for x in v] if isinstance(v, list) else [0]  # calculation.cpp:335-345
+        elif k in ("frozen_core", "deleted_virtual"):
             if isinstance(v, bool):
                 raise ValueError(f"ci_keywords.{k} must be a list of numbers")  # as calculation.cpp:374-389
             v = [int(x) for x in v]
@@ -96,10 +103,11 @@ def parse(data: Union[dict, str]) -> CIKeywords:
     return kw
 
 
-def run(kw: CIKeywords, problem: Optional[dict] = None, e_const: float = 0.0) -> dict:
+def run(kw: CIKeywords, problem: Optional[dict] = None, e_const: float = 0.0, mo_coeff=None) -> dict:
     """Solve one CI problem.  ``problem``: POLYQUANT_DETSET keyword arguments (integrals in the reference layout);
-    when None, the integrals come from ``kw.fcidump_filename``.  Returns energies (+ e_const), <S^2> when
-    requested, and the solver report."""
+    when None, the integrals come from ``kw.fcidump_filename``.  ``mo_coeff``: optional [species][spin] SCF
+    orbitals (n_ao x n_mo, frozen-core orbitals first as ``kw.frozen_core`` says) for the natural orbitals.
+    Returns energies (+ e_const), <S^2> when requested, natural orbitals and the solver report."""
     import torch
 
     from . import fcidump
@@ -142,6 +150,16 @@ def run(kw: CIKeywords, problem: Optional[dict] = None, e_const: float = 0.0) ->
         out["energies"] = (np.asarray(e) + e_const).tolist()
         if kw.calc_s2:
             out["s2"] = ds.s2(vecs).tolist()
+        states = [st for st in kw.NO_states if 0 <= st < k]
+        if states:
+            from .natural_orbitals import calculate_NOs
+
+            if mo_coeff is None:
+                C_combined, fc = [[np.eye(n)] for n in ds.n_orb], None
+            else:
+                C_combined = mo_coeff
+                fc = list(kw.frozen_core) + [0] * (ds.n_species - len(kw.frozen_core))
+            out["natural_orbitals"] = calculate_NOs(ds, vecs, C_combined, NO_states=states, frozen_core=fc)
     finally:
         ds.close()
     return out

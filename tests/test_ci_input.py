@@ -14,7 +14,7 @@ SAMPLE = {
             "convergence_E": 1e-8, "num_states": 2, "num_subspace_vec": 20, "slow_diag": False,
             "excitation_level": [[2, 2, 4]], "frozen_core": [0], "deleted_virtual": [0],
             "build_matrix": False, "calc_s2": True, "fcidump_filename": "INTEGRALS",
-            "spin_penalty_type": "first_order", "NO_states": [0], "precision": "mixed",
+            "spin_penalty_type": "first_order", "NO_states": [0, 1], "precision": "mixed",
         },
     },
 }
@@ -30,7 +30,8 @@ def test_parse_values_and_unsupported(tmp_path):
         assert kw.frozen_core == [0] and kw.deleted_virtual == [0]
         assert not kw.build_matrix and kw.calc_s2 and kw.precision == "mixed"
         assert kw.fcidump_filename == "INTEGRALS"
-        assert sorted(kw.unsupported) == ["NO_states", "spin_penalty_type"]
+        assert kw.NO_states == [0, 1]
+        assert kw.unsupported == ["spin_penalty_type"]
 
 
 def test_defaults_match_the_reference():
@@ -38,6 +39,7 @@ def test_defaults_match_the_reference():
     # epci.hpp:113-122, determinant_set.hpp:195-196
     assert (kw.convergence_E, kw.num_states, kw.num_subspace_vec, kw.iteration_max) == (1e-6, 1, 5, 500)
     assert kw.build_matrix and not kw.exact_diag and not kw.slow_diag
+    assert kw.NO_states == [0]  # calculation.cpp:335-345
     assert kw.excitation_levels(2) is None and kw.precision == "fp64"
 
 

@@ -33,6 +33,8 @@ def test_cisd_from_json_and_fcidump(integrals, extra):
     assert out["n_dets"] == 141
     assert np.abs(np.array(out["energies"]) - E_CISD).max() < 1e-6
     assert abs(out["s2"][0]) < 1e-6  # closed-shell ground state: a singlet
+    occ = out["natural_orbitals"]["occ_nso"][0][0][0]  # state 0, electrons, alpha (MO basis)
+    assert abs(occ.sum() - 5) < 1e-8 and np.all(np.diff(occ) <= 0)
 
 
 @pytest.mark.parametrize("extra", [{"build_matrix": True}, {"build_matrix": True, "exact_diag": True},
