@@ -15,6 +15,7 @@ reference keys its classical particles by symbol in a std::map
 """
 from __future__ import annotations
 
+import functools
 import itertools
 import math
 
@@ -51,7 +52,7 @@ BASES = {
 }
 # "pure": true in the reference inputs -> libint solid-harmonic p order m=-1,0,+1 = (y, z, x)
 P_ORDER_PURE = [(0, 1, 0), (0, 0, 1), (1, 0, 0)]
-Z = {"H": 1.0, "O": 8.0}
+Z = {"H": 1.0, "Li": 3.0, "O": 8.0}
 
 
 def boys(n: int, T: np.ndarray) -> np.ndarray:
@@ -97,6 +98,12 @@ def _R(t, u, v, n, p, PCx, PCy, PCz, RPC):
             val += (t - 1) * _R(t - 2, u, v, n + 1, p, PCx, PCy, PCz, RPC)
         val += PCx * _R(t - 1, u, v, n + 1, p, PCx, PCy, PCz, RPC)
     return val
+
+
+# The recursions are pure functions of their arguments; memoising them makes
+# the contracted integrals over repeated primitive pairs several times faster.
+_E = functools.lru_cache(maxsize=1 << 20)(_E)
+_R = functools.lru_cache(maxsize=1 << 20)(_R)
 
 
 class Prim:
@@ -243,6 +250,10 @@ class Molecule:
                 V[i, j] = V[j, i] = v
         return S, T, V
 
+    def eri_with(self, other: "Molecule") -> np.ndarray:
+        """(ij|kl) with i, j over this basis and k, l over ``other``'s (e.g. electron | positron)."""
+        return eri_cross(self.basis, other.basis)
+
     def eri(self) -> np.ndarray:
         n = self.nbf
         out = np.zeros((n, n, n, n))
@@ -261,6 +272,134 @@ class Molecule:
                                  (k, l, i, j), (l, k, i, j), (k, l, j, i), (l, k, j, i)):
                 out[a, b, c, d] = v
         return out
+
+
+def _contracted_eri(fa, fb, fc, fd) -> float:
+    v = 0.0
+    for pa in fa:
+        for pb in fb:
+            for pc in fc:
+                for pd in fd:
+                    v += pa.c * pb.c * pc.c * pd.c * _eri_prim(pa, pb, pc, pd)
+    return v
+
+
+def eri_cross(basis_a, basis_b) -> np.ndarray:
+    """Coulomb integrals (ij|kl) between two basis sets, i, j in ``basis_a`` and k, l in ``basis_b``."""
+    na, nb = len(basis_a), len(basis_b)
+    out = np.zeros((na, na, nb, nb))
+    for i in range(na):
+        for j in range(i + 1):
+            for k in range(nb):
+                for l in range(k + 1):
+                    v = _contracted_eri(basis_a[i], basis_a[j], basis_b[k], basis_b[l])
+                    out[i, j, k, l] = out[j, i, k, l] = out[i, j, l, k] = out[j, i, l, k] = v
+    return out
+
+
+def epscf(species, cross, e_nuc=0.0, conv=1e-12, max_iter=500):
+    """Multicomponent Hartree-Fock restating the reference's POLYQUANT_EPSCF fixed point
+    (src/scf/epscf.cpp): per species s and spin block,
+        F = H_core + J_ss(D_total,s) - K_ss(D_spin) + sum_t q_s q_t J_st(D_total,t)
+    with H_core = T / mass - q V (form_H_core, epscf.cpp:5-22), same-species Coulomb and exchange and
+    cross-species Coulomb only (form_fock_helper_single_fock_matrix, epscf.cpp:117-273; the density of a
+    restricted species with more than one particle is doubled for Coulomb, directscf_get_density_coulomb,
+    :82-103), aufbau occupations, and the energies of calculate_E_elec (:519-577).  Converged directly with
+    DIIS on F D S - S D F; the reference's staged start (species first independent, then coupled) reaches the
+    same fixed point for the ground states used here.
+
+    species: [dict(S, H, eri, n_alpha, n_beta, restricted, charge)], cross: {(0, 1): (ij|kl) with ij of
+    species 0 and kl of species 1}.  Returns (E_total, [dict(C, eps, D, F, E) per species]) where C, eps, D
+    and F are lists over spin blocks (one block for a restricted species or a single particle)."""
+    ns = len(species)
+    X = []
+    for sp in species:
+        w, U = np.linalg.eigh(sp["S"])
+        X.append(U @ np.diag(w ** -0.5) @ U.T)
+    nblk = [1 if (sp["restricted"] or sp["n_alpha"] + sp["n_beta"] == 1) else 2 for sp in species]
+    nocc = [[sp["n_alpha"], sp["n_beta"]][:nblk[k]] for k, sp in enumerate(species)]
+
+    def diag(F, k):
+        e, Cp = np.linalg.eigh(X[k].T @ F @ X[k])
+        return e, X[k] @ Cp
+
+    C = [[diag(species[k]["H"], k)[1] for _ in range(nblk[k])] for k in range(ns)]
+    eps = [[None] * nblk[k] for k in range(ns)]
+
+    def densities(C):
+        return [[C[k][b][:, :nocc[k][b]] @ C[k][b][:, :nocc[k][b]].T for b in range(nblk[k])] for k in range(ns)]
+
+    def total(D, k):
+        sp = species[k]
+        if nblk[k] == 2:
+            return D[k][0] + D[k][1]
+        return 2.0 * D[k][0] if sp["n_alpha"] + sp["n_beta"] > 1 else D[k][0]
+
+    def fock(D):
+        F = []
+        for k, sp in enumerate(species):
+            Jk = np.einsum("pqrs,rs->pq", sp["eri"], total(D, k), optimize=True)
+            G = sp["H"] + Jk
+            for t in range(ns):
+                if t == k:
+                    continue
+                qq = sp["charge"] * species[t]["charge"]
+                if (k, t) in cross:
+                    G = G + qq * np.einsum("pqrs,rs->pq", cross[(k, t)], total(D, t), optimize=True)
+                else:
+                    G = G + qq * np.einsum("rspq,rs->pq", cross[(t, k)], total(D, t), optimize=True)
+            F.append([G - np.einsum("prqs,rs->pq", sp["eri"], D[k][b], optimize=True) for b in range(nblk[k])])
+        return F
+
+    def energies(D, F):
+        E = []
+        for k, sp in enumerate(species):
+            H = sp["H"]
+            if sp["n_alpha"] + sp["n_beta"] == 1:
+                E.append(0.5 * np.sum(D[k][0] * (H + F[k][0])))
+            elif nblk[k] == 2:
+                E.append(0.5 * np.sum((D[k][0] + D[k][1]) * H + D[k][0] * F[k][0] + D[k][1] * F[k][1]))
+            else:
+                E.append(np.sum(D[k][0] * (H + F[k][0])))
+        return E
+
+    hist_F, hist_e = [], []
+    E_old = None
+    for _ in range(max_iter):
+        D = densities(C)
+        F = fock(D)
+        E = energies(D, F)
+        errs = [F[k][b] @ D[k][b] @ species[k]["S"] - species[k]["S"] @ D[k][b] @ F[k][b]
+                for k in range(ns) for b in range(nblk[k])]
+        err = max(float(np.abs(e).max()) for e in errs)
+        Et = sum(E) + e_nuc
+        if E_old is not None and abs(Et - E_old) < conv and err < 1e-10:
+            break
+        E_old = Et
+        hist_F.append(F)
+        hist_e.append(np.concatenate([e.ravel() for e in errs]))
+        hist_F, hist_e = hist_F[-10:], hist_e[-10:]
+        m = len(hist_F)
+        Fx = F
+        if m > 1:
+            B = -np.ones((m + 1, m + 1))
+            B[m, m] = 0.0
+            for a in range(m):
+                for b in range(m):
+                    B[a, b] = hist_e[a] @ hist_e[b]
+            rhs = np.zeros(m + 1)
+            rhs[m] = -1.0
+            coef = np.linalg.solve(B, rhs)[:m]
+            Fx = [[sum(c * hf[k][b] for c, hf in zip(coef, hist_F)) for b in range(nblk[k])] for k in range(ns)]
+        for k in range(ns):
+            for b in range(nblk[k]):
+                eps[k][b], C[k][b] = diag(Fx[k][b], k)
+    D = densities(C)
+    F = fock(D)
+    E = energies(D, F)
+    out = [dict(C=C[k], eps=[diag(F[k][b], k)[0] for b in range(nblk[k])], D=D[k], F=F[k], E=E[k])
+           for k in range(ns)]
+    return sum(E) + e_nuc, out
 
 
 def rhf(S, hcore, eri, n_occ, e_nuc, conv=1e-12, max_iter=200):

@@ -73,3 +73,51 @@ def h_minus():
     p = O.CIProblem([C.shape[1]], [1], [1], [[h, h]], {(0, 0, 0, 0): O.ao2mo_full(eri, C, C)}, [[1, 1, 2]],
                     restricted=[1], charge=[-1.0], e_const=mol.e_nuc())
     return dict(problem=p, C=C, S=S, E_rhf=E, no_occ=g["no_occ"], no_ao=g["no_ao"])
+
+
+def _shells(g, prefix):
+    return [("s" if g[prefix + "_kind"][i] == 0 else "p", list(g[prefix + "_exp"][i, :n]),
+             list(g[prefix + "_coef"][i, :n])) for i, n in enumerate(g[prefix + "_nprim"])]
+
+
+def ep_atom(symbol, e_shells, p_shells, n_e_alpha, n_e_beta, ex, max_coll=2 ** 31 - 1):
+    """One atom at the origin with electrons (restricted) and one positron (charge +1, mass 1): AO integrals
+    from the oracle's Gaussian-integral code, the multicomponent SCF, and the CI problem in the MO basis
+    (h = C^T (T - qV) C, integral.cpp:166-205; (ij|kl) blocks as calculate_mo_2_body_integrals fills them)."""
+    import gaussian_ints as G
+
+    me = G.Molecule([symbol], [0.0, 0.0, 0.0], {symbol: e_shells})
+    mp = G.Molecule([symbol], [0.0, 0.0, 0.0], {symbol: p_shells})
+    Se, Te, Ve = me.one_body()
+    Sp, Tp, Vp = mp.one_body()
+    eri_e = me.eri()
+    eri_p = eri_e if p_shells == e_shells else mp.eri()
+    eri_ep = eri_e if p_shells == e_shells else me.eri_with(mp)
+    He, Hp = Te + Ve, Tp - Vp   # T/mass - q V with q = -1 (electrons), +1 (positron), mass 1
+    spec = [dict(S=Se, H=He, eri=eri_e, n_alpha=n_e_alpha, n_beta=n_e_beta, restricted=True, charge=-1.0),
+            dict(S=Sp, H=Hp, eri=eri_p, n_alpha=1, n_beta=0, restricted=False, charge=1.0)]
+    E, res = G.epscf(spec, {(0, 1): eri_ep}, e_nuc=me.e_nuc())
+    Ce, Cp = res[0]["C"][0], res[1]["C"][0]
+    he, hp = Ce.T @ He @ Ce, Cp.T @ Hp @ Cp
+    eri = {(0, 0, 0, 0): O.ao2mo_full(eri_e, Ce, Ce), (1, 0, 1, 0): O.ao2mo_full(eri_p, Cp, Cp),
+           (0, 0, 1, 0): O.ao2mo_full(eri_ep, Ce, Cp)}
+    p = O.CIProblem([Ce.shape[1], Cp.shape[1]], [n_e_alpha, 1], [n_e_beta, 0], [[he, he], [hp, hp]], eri, ex,
+                    restricted=[1, 1], charge=[-1.0, 1.0], max_collective=max_coll, e_const=me.e_nuc())
+    return dict(problem=p, E_scf=E, scf=res, H_core=[He, Hp], C=[Ce, Cp])
+
+
+def li_wpos(ex=((1, 1, 1), (1, 1, 1))):
+    """Li- + e+ in the reference's Li_basis.g94 for both species (tests/data/li-_custombasis_wpos/Li_wpos.json)."""
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "positron_bases.npz"))
+    sh = _shells(g, "li")
+    return ep_atom("Li", sh, sh, 2, 2, [list(e) for e in ex])
+
+
+def psh_wpos(ex=((1, 1, 1), (1, 0, 1))):
+    """PsH: H, two electrons and a positron in the bases of tests/data/PsH_wpos/PsH_wpos_CI.json."""
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "positron_bases.npz"))
+    return ep_atom("H", _shells(g, "psh_e"), _shells(g, "psh_p"), 1, 1, [list(e) for e in ex])

@@ -17,6 +17,9 @@ Sources (paths inside the polyquant project):
     tests/data/PsH_wpos/h_minus_NO.txt       natural orbitals in the AO basis
         (compared in tests/unit_tests/ci/ci_test.cpp:854-871, "CI: Natural Orbitals";
          input tests/data/PsH_wpos/H_minus.json: RHF, CISD [1,1,2], state 0)
+  positron_bases.npz
+    tests/data/li-_custombasis_wpos/Li_basis.g94   s and p shells of Li_wpos.json (electron and positron)
+    tests/data/PsH_wpos/electron_basis.g94, positron_basis.g94   the bases of PsH_wpos_CI.json
 """
 import os
 
@@ -26,19 +29,32 @@ REF = os.environ.get("POLYQUANT_REF", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def read_g94_s_shells(path):
-    """(exponents, coefficients) of each shell of a Gaussian-94 basis file; s shells only."""
+def read_g94(path):
+    """[(kind, [(exponent, coefficient), ...]), ...] of a one-element Gaussian-94 basis file (s and p shells)."""
     shells = []
-    lines = [ln.split() for ln in open(path) if ln.strip() and not ln.startswith("*")]
+    lines = [ln.split() for ln in open(path) if ln.strip() and not ln.strip().startswith("*")]
     k = 1  # skip the element line
     while k < len(lines):
         kind, nprim = lines[k][0].lower(), int(lines[k][1])
-        if kind != "s":
-            raise ValueError(f"{path}: only s shells are read, found {kind}")
+        if kind not in ("s", "p"):
+            raise ValueError(f"{path}: only s and p shells are read, found {kind}")
         prims = [(float(a), float(c)) for a, c in (lines[k + 1 + i][:2] for i in range(nprim))]
-        shells.append(prims)
+        shells.append((kind, prims))
         k += 1 + nprim
     return shells
+
+
+def pack_shells(shells, prefix):
+    """Shells as padded arrays: <prefix>_kind (0 = s, 1 = p), _nprim, _exp, _coef."""
+    mp = max(len(p) for _, p in shells)
+    exps = np.zeros((len(shells), mp))
+    coefs = np.zeros((len(shells), mp))
+    for i, (_, prims) in enumerate(shells):
+        for j, (a, c) in enumerate(prims):
+            exps[i, j], coefs[i, j] = a, c
+    return {prefix + "_kind": np.array([0 if k == "s" else 1 for k, _ in shells], dtype=np.int32),
+            prefix + "_nprim": np.array([len(p) for _, p in shells], dtype=np.int32),
+            prefix + "_exp": exps, prefix + "_coef": coefs}
 
 
 def h2o():
@@ -53,21 +69,29 @@ def h2o():
 
 def h_minus():
     d = os.path.join(REF, "tests", "data", "PsH_wpos")
-    shells = read_g94_s_shells(os.path.join(d, "electron_basis.g94"))
-    mp = max(len(s) for s in shells)
-    exps = np.zeros((len(shells), mp))
-    coefs = np.zeros((len(shells), mp))
-    nprim = np.array([len(s) for s in shells], dtype=np.int32)
-    for i, s in enumerate(shells):
-        for j, (a, c) in enumerate(s):
-            exps[i, j], coefs[i, j] = a, c
+    shells = pack_shells(read_g94(os.path.join(d, "electron_basis.g94")), "shell")
     occ = np.loadtxt(os.path.join(d, "h_minus_NO_occ.txt"))
     no = np.loadtxt(os.path.join(d, "h_minus_NO.txt"))
     out = os.path.join(HERE, "h_minus_no_golden.npz")
-    np.savez_compressed(out, shell_exp=exps, shell_coef=coefs, shell_nprim=nprim, no_occ=occ, no_ao=no)
+    np.savez_compressed(out, shell_exp=shells["shell_exp"], shell_coef=shells["shell_coef"],
+                        shell_nprim=shells["shell_nprim"], no_occ=occ, no_ao=no)
+    print("wrote", out)
+
+
+def positron_bases():
+    """Basis sets of the reference's electron-positron inputs:
+    tests/data/li-_custombasis_wpos/Li_basis.g94 (electron and positron basis of Li_wpos.json) and
+    tests/data/PsH_wpos/{electron,positron}_basis.g94 (PsH_wpos_CI.json)."""
+    li = pack_shells(read_g94(os.path.join(REF, "tests", "data", "li-_custombasis_wpos", "Li_basis.g94")), "li")
+    d = os.path.join(REF, "tests", "data", "PsH_wpos")
+    pe = pack_shells(read_g94(os.path.join(d, "electron_basis.g94")), "psh_e")
+    pp = pack_shells(read_g94(os.path.join(d, "positron_basis.g94")), "psh_p")
+    out = os.path.join(HERE, "positron_bases.npz")
+    np.savez_compressed(out, **li, **pe, **pp)
     print("wrote", out)
 
 
 if __name__ == "__main__":
     h2o()
     h_minus()
+    positron_bases()
