@@ -159,8 +159,9 @@ pq_status pq_ci_sigma(pq_ci_handle *h, const double *C, int64_t ldc, int32_t nve
 pq_status pq_ci_sigma_host(pq_ci_handle *h, const double *C, int64_t ldc, int32_t nvec, double *S, int64_t lds,
                            int32_t precision) {
   clear_error();
-  if (!h || !C || !S || nvec < 1) {
-    set_error("pq_ci_sigma_host: bad arguments");
+  if (!h || !C || !S || nvec < 1 || ldc < h->n_dets || lds < h->n_dets) {
+    set_error("pq_ci_sigma_host: bad arguments (nvec=%d, ldc=%lld, lds=%lld, n_dets=%lld)", nvec, (long long)ldc,
+              (long long)lds, (long long)(h ? h->n_dets : 0));
     return PQ_ERR_ARG;
   }
   int64_t n = h->n_dets;
