@@ -1,6 +1,8 @@
 """Shared CI test cases (H2O/STO-3G from the oracle's integral code, seeded synthetics)."""
 from __future__ import annotations
 
+import functools
+
 import numpy as np
 
 import oracle as O
@@ -103,9 +105,11 @@ def ep_atom(symbol, e_shells, p_shells, n_e_alpha, n_e_beta, ex, max_coll=2 ** 3
            (0, 0, 1, 0): O.ao2mo_full(eri_ep, Ce, Cp)}
     p = O.CIProblem([Ce.shape[1], Cp.shape[1]], [n_e_alpha, 1], [n_e_beta, 0], [[he, he], [hp, hp]], eri, ex,
                     restricted=[1, 1], charge=[-1.0, 1.0], max_collective=max_coll, e_const=me.e_nuc())
-    return dict(problem=p, E_scf=E, scf=res, H_core=[He, Hp], C=[Ce, Cp])
+    return dict(problem=p, E_scf=E, scf=res, H_core=[He, Hp], C=[Ce, Cp],
+                ao=dict(eri_e=eri_e, eri_p=eri_p, eri_ep=eri_ep))
 
 
+@functools.lru_cache(maxsize=None)
 def li_wpos(ex=((1, 1, 1), (1, 1, 1))):
     """Li- + e+ in the reference's Li_basis.g94 for both species (tests/data/li-_custombasis_wpos/Li_wpos.json)."""
     import os
@@ -115,6 +119,7 @@ def li_wpos(ex=((1, 1, 1), (1, 1, 1))):
     return ep_atom("Li", sh, sh, 2, 2, [list(e) for e in ex])
 
 
+@functools.lru_cache(maxsize=None)
 def psh_wpos(ex=((1, 1, 1), (1, 0, 1))):
     """PsH: H, two electrons and a positron in the bases of tests/data/PsH_wpos/PsH_wpos_CI.json."""
     import os
