@@ -239,7 +239,8 @@ class Detset:
         L = lib()
         self._h = L.orc_detset_create(ctypes.byref(self._desc), 1 if check_addressing else 0)
         if not self._h:
-            raise ValueError("oracle detset creation failed (excitation level exceeds virtual size?)")
+            raise ValueError("oracle detset creation failed (excitation level exceeds the virtual orbitals, or an "
+                             "integral block is missing)")
         self.n_dets = L.orc_n_dets(self._h)
         self.n_words = L.orc_n_words(self._h)
         self.ntup = 2 * prob.n_species

@@ -310,8 +310,23 @@ orc_detset *orc_detset_create(const orc_desc *d, int check_addressing) {
     free(ds);
     return NULL;
   }
+  for (int s = 0; s < d->n_species; s++) ds->n_spin_blocks[s] = d->restricted[s] ? 1 : 2;
+  /* every integral block the element formulas read: h1 per spin block, and
+   * (a, sa | b, sb) for b >= a over both species' spin blocks */
+  for (int a = 0; a < d->n_species; a++)
+    for (int sa = 0; sa < ds->n_spin_blocks[a]; sa++) {
+      if (!d->h1[a][sa]) {
+        free(ds);
+        return NULL;
+      }
+      for (int b = a; b < d->n_species; b++)
+        for (int sb = 0; sb < ds->n_spin_blocks[b]; sb++)
+          if (!d->eri[a][sa][b][sb]) {
+            free(ds);
+            return NULL;
+          }
+    }
   for (int s = 0; s < d->n_species; s++) {
-    ds->n_spin_blocks[s] = d->restricted[s] ? 1 : 2;
     int ne[2] = {d->n_alpha[s], d->n_beta[s]};
     for (int sp = 0; sp < 2; sp++) {
       ds->n_str[s][sp] = make_strings(ds->n_words, d->n_orb[s], ne[sp], d->ex_level[s][sp], &ds->str[s][sp], &ds->lvl[s][sp]);

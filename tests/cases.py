@@ -51,6 +51,21 @@ def synthetic_ep(n_e, ne_a, ne_b, n_p, np_a, np_b, seed=0, ex_e=None, ex_p=None,
                        [ex_e, ex_p], restricted=[1, 1], charge=[-1.0, 1.0], max_collective=max_coll)
 
 
+def synthetic_en(n_e, ne_a, ne_b, n_n, nn_a, nn_b, seed=0, nuc_charge=2.0):
+    """Electrons + a quantum-nucleus species with unrestricted (different alpha and beta) integral blocks and
+    charge ``nuc_charge``: cross-species terms carry charge[0] * charge[1] = -nuc_charge, and the nuclear
+    alpha-alpha, beta-beta, alpha-beta and electron-nucleus blocks are all distinct."""
+    h_e, h_na, ee, nna, en_a = synthetic.ep_integrals(n_e, n_n, seed)
+    _, h_nb, _, nnb, en_b = synthetic.ep_integrals(n_e, n_n, seed + 1)
+    nn_ab = 0.5 * (nna + nnb)
+    ex_e = [min(ne_a, n_e - ne_a), min(ne_b, n_e - ne_b), min(ne_a, n_e - ne_a) + min(ne_b, n_e - ne_b)]
+    ex_n = [min(nn_a, n_n - nn_a), min(nn_b, n_n - nn_b), min(nn_a, n_n - nn_a) + min(nn_b, n_n - nn_b)]
+    eri = {(0, 0, 0, 0): ee, (1, 0, 1, 0): nna, (1, 1, 1, 1): nnb, (1, 0, 1, 1): nn_ab, (1, 1, 1, 0): nn_ab.T,
+           (0, 0, 1, 0): en_a, (0, 0, 1, 1): en_b}
+    return O.CIProblem([n_e, n_n], [ne_a, nn_a], [ne_b, nn_b], [[h_e, h_e], [h_na, h_nb]], eri, [ex_e, ex_n],
+                       restricted=[1, 0], charge=[-1.0, nuc_charge])
+
+
 def batch_dict(p):
     """CIProblem -> keyword dict of CIBatch / POLYQUANT_DETSET."""
     return dict(n_orb=p.n_orb, n_alpha=p.n_alpha, n_beta=p.n_beta, h1=p.h1, eri=p.eri, excitation_level=p.ex_level,

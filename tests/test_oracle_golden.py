@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from cases import h2o_problem, synthetic_ep, synthetic_fci, synthetic_unrestricted
+from cases import h2o_problem, synthetic_en, synthetic_ep, synthetic_fci, synthetic_unrestricted
 
 LOOSE, TIGHT, XTIGHT = 1e-6, 1e-8, 1e-14
 
@@ -223,7 +223,7 @@ def test_sigma_fast_vs_slow_h2o_cisd(h2o):
         assert np.abs(fast - slow).max() < 10 * XTIGHT * max(1.0, np.abs(slow).max())
 
 
-@pytest.mark.parametrize("kind", ["fci", "unrestricted", "ep_cis", "ep_full"])
+@pytest.mark.parametrize("kind", ["fci", "unrestricted", "ep_cis", "ep_full", "e_nucleus_unrestricted"])
 def test_sigma_fast_vs_slow_synthetic(kind):
     if kind == "fci":
         p = synthetic_fci(7, 3, 2, seed=3)
@@ -231,8 +231,10 @@ def test_sigma_fast_vs_slow_synthetic(kind):
         p = synthetic_unrestricted(6, 3, 2, seed=5)
     elif kind == "ep_cis":
         p = synthetic_ep(6, 2, 1, 5, 1, 0, seed=2, ex_e=[1, 1, 1], ex_p=[1, 1, 1])
-    else:
+    elif kind == "ep_full":
         p = synthetic_ep(5, 2, 2, 4, 1, 1, seed=4, max_coll=3)
+    else:
+        p = synthetic_en(5, 2, 1, 4, 1, 1, seed=6, nuc_charge=2.0)
     ds = O.Detset(p)
     rng = np.random.default_rng(1)
     C = rng.standard_normal((ds.n_dets, 3))
@@ -249,4 +251,13 @@ def test_sigma_fast_vs_slow_synthetic(kind):
 def test_excitation_level_exceeds_virtuals_is_an_error():
     p = synthetic_fci(5, 3, 3, seed=0, ex=[3, 3, 6])
     with pytest.raises(ValueError):
+        O.Detset(p)
+
+
+def test_missing_integral_block_is_an_error():
+    from cases import synthetic_en
+
+    p = synthetic_en(4, 1, 1, 3, 1, 1, seed=1)
+    del p.eri[(1, 1, 1, 0)]
+    with pytest.raises(ValueError, match="integral block"):
         O.Detset(p)
