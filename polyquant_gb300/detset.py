@@ -229,6 +229,16 @@ class POLYQUANT_DETSET:
               "pq_ci_rdm1")
         return out
 
+    # the reference's names and argument order for the same two properties
+    def evaluate_s2(self, C) -> np.ndarray:
+        """S_squared (n_states x n_species) as POLYQUANT_DETSET::evaluate_s2 fills it (s2.cpp:4-123)."""
+        return np.asarray(self.s2(C)).reshape(-1, self.n_species)
+
+    def create_1rdm(self, state_idx: int, quantum_part_idx: int, quantum_part_spin_idx: int, C) -> np.ndarray:
+        """MO_rdm1 of column state_idx of C as POLYQUANT_DETSET::create_1rdm computes it (rdm1.cpp:4-72)."""
+        c = C[:, state_idx] if C.dim() == 2 else C
+        return self.rdm1(c, spin=quantum_part_spin_idx, species=quantum_part_idx)
+
     def release_ham(self):
         check(_lib.load().pq_ci_ham_release(self._h))
 
