@@ -22,18 +22,35 @@ _LIB_PATH = os.path.join(_BUILD, "libpq_oracle.so")
 _lib = None
 
 
+_REFALG_PATH = os.path.join(_BUILD, "libpq_refalg.so")
+_refalg = None
+
+
 def build(force: bool = False) -> str:
     """Compile the C oracle into ``oracle/_build/libpq_oracle.so`` (gcc + OpenMP)."""
     src = os.path.join(_HERE, "pq_oracle.c")
     hdr = os.path.join(_HERE, "pq_oracle.h")
-    if (not force and os.path.exists(_LIB_PATH)
-            and os.path.getmtime(_LIB_PATH) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
-        return _LIB_PATH
-    os.makedirs(_BUILD, exist_ok=True)
-    tmp = _LIB_PATH + f".tmp{os.getpid()}"
-    subprocess.check_call(["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-o", tmp, src])
-    os.replace(tmp, _LIB_PATH)
+    if (force or not os.path.exists(_LIB_PATH)
+            or os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(src), os.path.getmtime(hdr))):
+        os.makedirs(_BUILD, exist_ok=True)
+        tmp = _LIB_PATH + f".tmp{os.getpid()}"
+        subprocess.check_call(["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-o", tmp, src])
+        os.replace(tmp, _LIB_PATH)
     return _LIB_PATH
+
+
+def build_refalg(force: bool = False) -> str:
+    """Compile the reference-faithful sigma restatement (ref_restated.cpp) into ``oracle/_build/libpq_refalg.so``
+    (g++ + OpenMP, linked against the oracle); built on first use only."""
+    build()
+    ref = os.path.join(_HERE, "ref_restated.cpp")
+    if (force or not os.path.exists(_REFALG_PATH)
+            or os.path.getmtime(_REFALG_PATH) < max(os.path.getmtime(ref), os.path.getmtime(_LIB_PATH))):
+        tmp = _REFALG_PATH + f".tmp{os.getpid()}"
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-I", _HERE, "-o", tmp,
+                               ref, "-L", _BUILD, "-lpq_oracle", "-Wl,-rpath,$ORIGIN"])
+        os.replace(tmp, _REFALG_PATH)
+    return _REFALG_PATH
 
 
 class OrcDesc(ctypes.Structure):
@@ -330,6 +347,41 @@ class Detset:
         r = np.ascontiguousarray(np.asarray(rows, dtype=np.int64))
         S = np.zeros((len(r), C.shape[1]), dtype=np.float64, order="F")
         lib().orc_sigma_rows(self._h, _ptr(C), self.n_dets, C.shape[1], _ptr(r), len(r), _ptr(S), nthreads)
+        return S
+
+
+class RefAlgDetset:
+    """The reference's one-species sigma with its own data structures (hash-map determinant index, linear
+    det_idx_unfold by every thread, per-thread private sigma, critical merge; ref_restated.cpp), for timing the
+    reference algorithm and for checking it against the oracle."""
+
+    def __init__(self, prob: CIProblem):
+        global _refalg
+        lib()  # the oracle library it links against
+        if _refalg is None:
+            _refalg = ctypes.CDLL(build_refalg())
+            _refalg.refalg_create.restype = ctypes.c_void_p
+            _refalg.refalg_create.argtypes = [ctypes.POINTER(OrcDesc)]
+            _refalg.refalg_destroy.argtypes = [ctypes.c_void_p]
+            _refalg.refalg_n_dets.restype = ctypes.c_int64
+            _refalg.refalg_n_dets.argtypes = [ctypes.c_void_p]
+            _refalg.refalg_sigma.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
+                                             ctypes.c_void_p, ctypes.c_int64, ctypes.c_int]
+        self._desc, self._keep = prob.orc_desc()
+        self._h = _refalg.refalg_create(ctypes.byref(self._desc))
+        if not self._h:
+            raise ValueError("reference restatement: one species only, with complete integral blocks")
+        self.n_dets = _refalg.refalg_n_dets(self._h)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _refalg.refalg_destroy(self._h)
+            self._h = None
+
+    def sigma(self, C: np.ndarray, nthreads: int = 0) -> np.ndarray:
+        C = np.asfortranarray(np.asarray(C, dtype=np.float64).reshape(self.n_dets, -1))
+        S = np.zeros_like(C, order="F")
+        _refalg.refalg_sigma(self._h, _ptr(C), self.n_dets, C.shape[1], _ptr(S), self.n_dets, nthreads)
         return S
 
 
