@@ -12,6 +12,7 @@ with libint).
 from __future__ import annotations
 
 import ctypes
+from typing import Dict, List, Sequence, Tuple
 
 from . import _lib
 from ._lib import PQ_AO_PACKED8, PQ_AO_PAIRS, PQ_XFORM_BF16X3, PQ_XFORM_FP64, PQ_XFORM_TF32X3, check  # noqa: F401
@@ -73,3 +74,32 @@ def calculate_mo_1_body_integrals(F_ao, mo_coeffs, frozen_core: int = 0, deleted
     check(_lib.load().pq_mo1(ctypes.c_void_p(F.data_ptr()), n, ctypes.c_void_p(C.data_ptr()), n, nmo,
                              ctypes.c_void_p(out.data_ptr()), st), "pq_mo1")
     return out.t()
+
+
+def calculate_mo_2_body_integrals(mo_coeffs: Sequence[Sequence], frozen_core: Sequence[int],
+                                  deleted_virtual: Sequence[int], eri_ao: Dict[Tuple[int, int], object],
+                                  num_parts: Sequence[Tuple[int, int]] = None, layout: int = PQ_AO_PACKED8,
+                                  mode: int = PQ_XFORM_FP64) -> List[List[List[List[object]]]]:
+    """mo_two_body_ints[a][sa][b][sb] for every species pair b >= a and every spin block of each
+    (calculate_mo_2_body_integrals, integral.cpp:479-516; entries with b < a stay None, as the reference leaves
+    them empty).  mo_coeffs[s][spin]: (n_ao x n_mo) device tensors, one per spin block; eri_ao[(a, b)]: the AO
+    integrals of the species pair in ``layout``; num_parts[s] = (alpha, beta) particle counts, passed through
+    as the reference does."""
+    ns = len(mo_coeffs)
+    parts = num_parts if num_parts is not None else [(0, 0)] * ns
+    out: List[List[List[List[object]]]] = []
+    for a in range(ns):
+        per_a = []
+        for sa in range(len(mo_coeffs[a])):
+            per_b = []
+            for b in range(ns):
+                blocks = [None] * len(mo_coeffs[b])
+                if b >= a:
+                    for sb in range(len(mo_coeffs[b])):
+                        blocks[sb] = transform_mo_2_body_integrals(
+                            a, b, mo_coeffs[a][sa], mo_coeffs[b][sb], parts[a][sa], parts[b][sb], frozen_core,
+                            deleted_virtual, eri_ao[(a, b)], layout=layout, mode=mode)
+                per_b.append(blocks)
+            per_a.append(per_b)
+        out.append(per_a)
+    return out
