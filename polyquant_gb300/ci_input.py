@@ -11,8 +11,9 @@ silently dropped.
 
 ``run`` solves one CI problem as ``POLYQUANT_EPCI::run`` would
 (src/ci/epci.cpp:575-686): the explicit sparse Hamiltonian when
-``build_matrix`` is set (the reference default), dense diagonalisation for
-``exact_diag``, block Davidson otherwise, <S^2> per state and species for
+``build_matrix`` is set (the reference default), dense diagonalisation of it
+for ``exact_diag`` (ignored without ``build_matrix``, as in the reference),
+block Davidson otherwise, <S^2> per state and species for
 ``calc_s2``, and the natural spin orbitals of the ``NO_states`` (default
 [0]; calculate_NOs, epci.cpp:200-318) in the basis of the caller's SCF
 orbitals, or in the MO basis when none are given.
@@ -130,9 +131,7 @@ def run(kw: CIKeywords, problem: Optional[dict] = None, e_const: float = 0.0, mo
     try:
         if kw.build_matrix:
             out["nnz"] = ds.create_ham(screening_threshold=kw.screening_threshold, use_for_sigma=True)
-        if kw.exact_diag:
-            if not kw.build_matrix:
-                raise ValueError("exact_diag needs build_matrix")
+        if kw.exact_diag and kw.build_matrix:  # exact_diag acts only on the explicit matrix (epci.cpp:605-633)
             rp, col, val = ds.ham_csr(upper=False)
             H = np.zeros((ds.N_dets, ds.N_dets))
             for i in range(ds.N_dets):
