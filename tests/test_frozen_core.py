@@ -68,3 +68,15 @@ def test_li_wpos_frozen_electron_core():
     assert act.n_dets == n_kept
     w_act = np.linalg.eigvalsh(act.dense_ham()) + E_fc[0]
     assert np.abs(w_act - w_full).max() < 1e-9
+
+
+def test_frozen_core_energy_reference_value(h2o):
+    """tests/unit_tests/ci/ci_test.cpp:132-146: H2O/STO-3G (file basis), two frozen orbitals,
+    frozen_core_energy = -71.3745646924 (1e-6)."""
+    r = h2o("file")
+    C, T, V, eri = r["C"], r["T"], r["V"], r["eri"]
+    Dfc = frozen_core_density(C, 2)
+    F = calculate_frozen_core_ints([T + V], [[Dfc]], [2], {(0, 0): eri}, [-1.0], [True])
+    assert abs(frozen_core_energy([T + V], [[Dfc]], F, [2], [True])[0] - -71.3745646924) < 1e-6
+    # nothing frozen: zero, as ci_test.cpp:148-163 requires
+    assert frozen_core_energy([T + V], [[0 * Dfc]], F, [0], [True]) == [0.0]

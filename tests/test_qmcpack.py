@@ -79,3 +79,14 @@ def test_payload_two_species():
     assert all(int(pl["CI_2"][k, 0]) == pos[u[k, 2]] for k in range(d.n_dets))
     assert np.all(pl["CI_3"] == 0)  # no beta positron
     assert int(pl["nstate"]) == 5
+
+
+def test_reference_get_det_withfcorbs_cases():
+    """tests/unit_tests/ci/ci_test.cpp:148-211: with two frozen orbitals the active HF string 00111 becomes
+    0011111; with max_orb = 75 the two-word string {0, 2^63 + 1} (highest word first) becomes {2, 7}."""
+    got = strings_with_frozen_core(np.array([0b00111], dtype=np.uint64), 2, 1)
+    assert int(got[0, 0]) == 0b0011111
+    assert int(strings_with_frozen_core(np.array([0b0011111], dtype=np.uint64), 0, 1)[0, 0]) == 0b0011111
+    n_words = ((75 + 2) >> 6) + 1
+    got = strings_with_frozen_core(np.array([(1 << 63) + 1], dtype=np.uint64), 2, n_words)
+    assert [int(x) for x in got[0][::-1]] == [2, 7]
