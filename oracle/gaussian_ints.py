@@ -230,7 +230,10 @@ class Molecule:
     def n_electrons(self) -> int:
         return int(sum(Z[s] for s, _ in self.atoms))
 
-    def one_body(self):
+    def one_body(self, nuclear_charges=None):
+        """(S, T, V); V attracts to every atom with charge Z[symbol], or with ``nuclear_charges[symbol]`` when
+        given (0 for a ghost centre, e.g. a nucleus treated as a quantum particle)."""
+        zc = Z if nuclear_charges is None else nuclear_charges
         n = self.nbf
         S = np.zeros((n, n))
         T = np.zeros((n, n))
@@ -244,7 +247,8 @@ class Molecule:
                         s += cc * _overlap_prim(p1, p2)
                         t += cc * _kinetic_prim(p1, p2)
                         for sym, C in self.atoms:
-                            v -= cc * Z[sym] * _nuclear_prim(p1, p2, C)
+                            if zc[sym] != 0.0:
+                                v -= cc * zc[sym] * _nuclear_prim(p1, p2, C)
                 S[i, j] = S[j, i] = s
                 T[i, j] = T[j, i] = t
                 V[i, j] = V[j, i] = v
@@ -297,14 +301,18 @@ def eri_cross(basis_a, basis_b) -> np.ndarray:
     return out
 
 
-def epscf(species, cross, e_nuc=0.0, conv=1e-12, max_iter=500):
+def epscf(species, cross, e_nuc=0.0, conv=1e-12, max_iter=500, cross_repeat_unrestricted=False):
     """Multicomponent Hartree-Fock restating the reference's POLYQUANT_EPSCF fixed point
     (src/scf/epscf.cpp): per species s and spin block,
         F = H_core + J_ss(D_total,s) - K_ss(D_spin) + sum_t q_s q_t J_st(D_total,t)
     with H_core = T / mass - q V (form_H_core, epscf.cpp:5-22), same-species Coulomb and exchange and
     cross-species Coulomb only (form_fock_helper_single_fock_matrix, epscf.cpp:117-273; the density of a
     restricted species with more than one particle is doubled for Coulomb, directscf_get_density_coulomb,
-    :82-103), aufbau occupations, and the energies of calculate_E_elec (:519-577).  Converged directly with
+    :82-103), aufbau occupations, and the energies of calculate_E_elec (:519-577).  With
+    ``cross_repeat_unrestricted`` the cross-species Coulomb term of a partner species with two spin blocks is
+    added once per block, as form_fock_helper (:275-307) does when it loops over the partner's spin blocks with
+    the partner's total density each time (so twice); the reference's quantum-nucleus SCF values carry this
+    double count.  Converged directly with
     DIIS on F D S - S D F; the reference's staged start (species first independent, then coupled) reaches the
     same fixed point for the ground states used here.
 
@@ -344,6 +352,8 @@ def epscf(species, cross, e_nuc=0.0, conv=1e-12, max_iter=500):
                 if t == k:
                     continue
                 qq = sp["charge"] * species[t]["charge"]
+                if cross_repeat_unrestricted and nblk[t] == 2:
+                    qq *= 2.0  # the reference adds the partner's Coulomb term once per spin block
                 if (k, t) in cross:
                     G = G + qq * np.einsum("pqrs,rs->pq", cross[(k, t)], total(D, t), optimize=True)
                 else:

@@ -141,3 +141,35 @@ def psh_wpos(ex=((1, 1, 1), (1, 0, 1))):
 
     g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "positron_bases.npz"))
     return ep_atom("H", _shells(g, "psh_e"), _shells(g, "psh_p"), 1, 1, [list(e) for e in ex])
+
+
+@functools.lru_cache(maxsize=None)
+def quantum_h_water(ex_n=(1, 1, 1), ex_e=(1, 1, 1)):
+    """H2O/STO-3G with both protons quantum (tests/data/h2o_sto3g_quantumHfile/h2o.json): species 0 = the two
+    protons (mass 1.00782503223, charge +1, restricted 1a1b; the reference orders species by name and "H"
+    sorts before "electron"), species 1 = the ten electrons (unrestricted 5a5b), both in the STO-3G basis on all
+    three centres; only the oxygen nucleus is a classical charge.  SCF through the oracle's multicomponent
+    restatement with the reference's per-spin-block cross-species Coulomb count; CI problem in the MO basis
+    with separate electron alpha and beta orbitals."""
+    import gaussian_ints as G
+
+    mol = G.Molecule(G.H2O_SYMBOLS, G.H2O_GEOMETRY, "file")
+    S, T, V = mol.one_body(nuclear_charges={"H": 0.0, "O": 8.0})
+    eri = mol.eri()
+    m_h = 1.00782503223
+    Hn, He = T / m_h - V, T + V
+    spec = [dict(S=S, H=Hn, eri=eri, n_alpha=1, n_beta=1, restricted=True, charge=1.0),
+            dict(S=S, H=He, eri=eri, n_alpha=5, n_beta=5, restricted=False, charge=-1.0)]
+    E, res = G.epscf(spec, {(0, 1): eri}, e_nuc=0.0, cross_repeat_unrestricted=True)
+    Cn = res[0]["C"][0]
+    Ca, Cb = res[1]["C"]
+    h_n = Cn.T @ Hn @ Cn
+    h_a, h_b = Ca.T @ He @ Ca, Cb.T @ He @ Cb
+    mo = O.ao2mo_full
+    eri_mo = {(0, 0, 0, 0): mo(eri, Cn, Cn),
+              (1, 0, 1, 0): mo(eri, Ca, Ca), (1, 1, 1, 1): mo(eri, Cb, Cb),
+              (1, 0, 1, 1): mo(eri, Ca, Cb), (1, 1, 1, 0): mo(eri, Cb, Ca),
+              (0, 0, 1, 0): mo(eri, Cn, Ca), (0, 0, 1, 1): mo(eri, Cn, Cb)}
+    p = O.CIProblem([7, 7], [1, 5], [1, 5], [[h_n, h_n], [h_a, h_b]], eri_mo, [list(ex_n), list(ex_e)],
+                    restricted=[1, 0], charge=[1.0, -1.0])
+    return dict(problem=p, E_scf=E, scf=res, H_core=[Hn, He], S=S, eri=eri)
