@@ -19,11 +19,18 @@ the CI):
 The active-space one-body integrals are then C_act^T F_fc C_act
 (``integral.calculate_mo_1_body_integrals`` on the device), and the CI
 energies are shifted by E_nuc + sum of the frozen-core energies
-(epci.cpp:595-614).  The reference's compute_frozen_core_ints converts the
-charge product to an integer and, for an unrestricted partner species with
-two spin blocks, adds its cross-species Coulomb term once per block; charges
-of +-1 and restricted or single-block partners (every input the reference
-ships) are unaffected, and this module takes the total density once.
+(epci.cpp:595-614).
+
+Two details of the reference's compute_frozen_core_ints are reproduced by
+default, so that the results equal the reference's on the same inputs: the
+charge product is converted to an integer, and the cross-species Coulomb
+term of a partner species with two spin blocks (unrestricted) is added once
+per block, each time with the partner's total frozen density -- the same
+per-block count the reference's SCF Fock build makes.  With
+``single_count_cross=True`` the partner's density enters once with the exact
+charge product (the physical operator, for which the frozen-block identity
+of the tests holds).  Restricted or single-block partners with charges of +-1
+are the same either way.
 """
 from __future__ import annotations
 
@@ -51,7 +58,8 @@ def _cross(eri_ao: Dict[Tuple[int, int], np.ndarray], a: int, b: int, D: np.ndar
 
 def calculate_frozen_core_ints(hcore: Sequence[np.ndarray], fc_dm: Sequence[Sequence[np.ndarray]],
                                frozen_core: Sequence[int], eri_ao: Dict[Tuple[int, int], np.ndarray],
-                               charge: Sequence[float], restricted: Sequence[bool]) -> List[List[np.ndarray]]:
+                               charge: Sequence[float], restricted: Sequence[bool],
+                               single_count_cross: bool = False) -> List[List[np.ndarray]]:
     """F_fc[a][spin] in the AO basis.
 
     hcore[a]      T / mass - charge * V of species a (AO, n_a x n_a)
@@ -72,8 +80,11 @@ def calculate_frozen_core_ints(hcore: Sequence[np.ndarray], fc_dm: Sequence[Sequ
                     f += _cross(eri_ao, a, a, Dt)
                     Ds = fc_dm[a][0] if restricted[a] else fc_dm[a][s]
                     f -= np.einsum("ikjl,kl->ij", eri_ao[(a, a)], Ds, optimize=True)
-                else:
+                elif single_count_cross:
                     f += charge[a] * charge[b] * _cross(eri_ao, a, b, Dt)
+                else:
+                    blocks = 1 if restricted[b] else len(fc_dm[b])
+                    f += blocks * int(charge[a] * charge[b]) * _cross(eri_ao, a, b, Dt)
             Fa.append(f)
         F.append(Fa)
     return F

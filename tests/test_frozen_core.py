@@ -80,3 +80,38 @@ def test_frozen_core_energy_reference_value(h2o):
     assert abs(frozen_core_energy([T + V], [[Dfc]], F, [2], [True])[0] - -71.3745646924) < 1e-6
     # nothing frozen: zero, as ci_test.cpp:148-163 requires
     assert frozen_core_energy([T + V], [[0 * Dfc]], F, [0], [True]) == [0.0]
+
+
+def test_unrestricted_frozen_core_with_a_nucleus_species():
+    """Quantum-proton water (protons species 0, UHF electrons species 1), electron 1s-like orbital frozen in
+    both spin blocks.  The reference's operator adds the electrons' frozen Coulomb field to the proton operator
+    once per electron spin block; the single-count operator satisfies the frozen-block identity."""
+    from cases import quantum_h_water
+
+    qh = quantum_h_water()
+    full = O.Detset(qh["problem"])
+    w_full, n_kept = frozen_block_spectrum(full, [2, 3], 1)
+    n, e = qh["scf"]
+    (Hn, He), eri = qh["H_core"], qh["eri"]
+    Cn, (Ca, Cb) = n["C"][0], e["C"]
+    fc_dm = [[np.zeros_like(Hn)], [frozen_core_density(Ca, 1), frozen_core_density(Cb, 1)]]
+    eris = {(0, 0): eri, (1, 1): eri, (0, 1): eri}
+    F_ref = calculate_frozen_core_ints([Hn, He], fc_dm, [0, 1], eris, [1.0, -1.0], [True, False])
+    F = calculate_frozen_core_ints([Hn, He], fc_dm, [0, 1], eris, [1.0, -1.0], [True, False],
+                                   single_count_cross=True)
+    cross = -np.einsum("ijkl,kl->ij", eri, fc_dm[1][0] + fc_dm[1][1])
+    assert np.abs(F_ref[0][0] - F[0][0] - cross).max() < 1e-12
+    assert all(np.array_equal(F_ref[1][s], F[1][s]) for s in range(2))
+    E_fc = frozen_core_energy([Hn, He], fc_dm, F, [0, 1], [True, False])
+    assert E_fc[0] == 0.0
+    Ca_, Cb_ = Ca[:, 1:], Cb[:, 1:]
+    mo = O.ao2mo_full
+    eri_act = {(0, 0, 0, 0): mo(eri, Cn, Cn), (1, 0, 1, 0): mo(eri, Ca_, Ca_), (1, 1, 1, 1): mo(eri, Cb_, Cb_),
+               (1, 0, 1, 1): mo(eri, Ca_, Cb_), (1, 1, 1, 0): mo(eri, Cb_, Ca_),
+               (0, 0, 1, 0): mo(eri, Cn, Ca_), (0, 0, 1, 1): mo(eri, Cn, Cb_)}
+    hn = Cn.T @ F[0][0] @ Cn
+    act = O.Detset(O.CIProblem([7, 6], [1, 4], [1, 4], [[hn, hn], [Ca_.T @ F[1][0] @ Ca_, Cb_.T @ F[1][1] @ Cb_]],
+                               eri_act, [[1, 1, 1], [1, 1, 1]], restricted=[1, 0], charge=[1.0, -1.0]))
+    assert act.n_dets == n_kept
+    w_act = np.linalg.eigvalsh(act.dense_ham()) + E_fc[1]
+    assert np.abs(w_act - w_full).max() < 1e-9
