@@ -144,8 +144,9 @@ def psh_wpos(ex=((1, 1, 1), (1, 0, 1))):
 
 
 @functools.lru_cache(maxsize=None)
-def quantum_h_water(ex_n=(1, 1, 1), ex_e=(1, 1, 1)):
-    """H2O/STO-3G with both protons quantum (tests/data/h2o_sto3g_quantumHfile/h2o.json): species 0 = the two
+def quantum_h_water(ex_n=(1, 1, 1), ex_e=(1, 1, 1), basis="file"):
+    """H2O/STO-3G with both protons quantum (tests/data/h2o_sto3g_quantumH{file,library}/h2o.json, ``basis`` the
+    file or library STO-3G digits): species 0 = the two
     protons (mass 1.00782503223, charge +1, restricted 1a1b; the reference orders species by name and "H"
     sorts before "electron"), species 1 = the ten electrons (unrestricted 5a5b), both in the STO-3G basis on all
     three centres; only the oxygen nucleus is a classical charge.  SCF through the oracle's multicomponent
@@ -153,7 +154,7 @@ def quantum_h_water(ex_n=(1, 1, 1), ex_e=(1, 1, 1)):
     with separate electron alpha and beta orbitals."""
     import gaussian_ints as G
 
-    mol = G.Molecule(G.H2O_SYMBOLS, G.H2O_GEOMETRY, "file")
+    mol = G.Molecule(G.H2O_SYMBOLS, G.H2O_GEOMETRY, basis)
     S, T, V = mol.one_body(nuclear_charges={"H": 0.0, "O": 8.0})
     eri = mol.eri()
     m_h = 1.00782503223

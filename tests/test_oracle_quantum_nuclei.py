@@ -1,5 +1,5 @@
 """Electron-nucleus known answers: H2O/STO-3G with both protons quantum
-(tests/data/h2o_sto3g_quantumHfile/h2o.json, tests/integration_tests/calculation/calculation_test.cpp:196-213),
+(tests/data/h2o_sto3g_quantumH{file,library}/h2o.json, tests/integration_tests/calculation/calculation_test.cpp:174-213),
 reproduced through the oracle's integral code and multicomponent SCF, then the CI path on that system.
 
 The reference's SCF adds the Coulomb term of an unrestricted partner species (here the electrons, 5a5b) once
@@ -21,7 +21,10 @@ def qh():
     return quantum_h_water()
 
 
-def test_quantum_proton_scf(qh):
+@pytest.mark.parametrize("basis", ["file", "library"])
+def test_quantum_proton_scf(basis):
+    """calculation_test.cpp:174-213: the same values for the file and the library STO-3G digits."""
+    qh = quantum_h_water(basis=basis)
     n, e = qh["scf"]
     assert abs(qh["E_scf"] - -78.1165107917) < LOOSE
     assert abs(n["E"] - 3.0365625787) < LOOSE and abs(e["E"] - -81.1530733704) < LOOSE
