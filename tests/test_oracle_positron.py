@@ -68,3 +68,14 @@ def test_psh_natural_spin_orbitals():
     Ce, Cp = np.abs(no["C_nso"][0][0][0][:, 0]), np.abs(no["C_nso"][0][1][0][:, 0])
     assert np.abs(Ce - [0.300771, 0.345285, 0.43364, 0.0889083, 0.00747211]).max() < LOOSE
     assert abs(Cp[0] - 1.36173) < 10 * LOOSE and abs(Cp[1] - 0.428029) < LOOSE
+
+
+def test_psh_multispecies_sigma_fast_vs_slow():
+    """ci_test.cpp:770-852: PsH_wpos.json bases, excitation level (1,1,1) for both species, sigma of e0, e5 and
+    the uniform vector by the pair-once builder equals the dense builder to 10 * 1e-14."""
+    p = psh_wpos(ex=((1, 1, 1), (1, 1, 1)))["problem"]
+    d = O.Detset(p)
+    n = d.n_dets
+    for C in (np.eye(n)[:, [0]], np.eye(n)[:, [5]], np.full((n, 1), 1.0 / n)):
+        fast, slow = d.sigma(C), d.sigma(C, slow=True)
+        assert np.abs(fast - slow).max() < 10 * 1e-14
