@@ -14,7 +14,7 @@ from typing import Dict, List, Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import PQ_FP32, PQ_FP64, check
+from ._lib import PQ_FP32, PQ_FP64, check  # noqa: F401  (PQ_FP32 re-exported for callers)
 from .detset import INT_MAX, make_desc
 
 

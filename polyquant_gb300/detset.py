@@ -13,12 +13,12 @@ levels {alpha, beta, total} per species and the collective limit.
 from __future__ import annotations
 
 import ctypes
-from typing import Dict, Optional, Sequence, Tuple
+from typing import Dict, Sequence
 
 import numpy as np
 
 from . import _lib
-from ._lib import PQ_FP32, PQ_FP64, check
+from ._lib import PQ_FP32, PQ_FP64, check  # noqa: F401  (PQ_FP32 re-exported for callers)
 
 INT_MAX = 2 ** 31 - 1
 

@@ -9,7 +9,6 @@ already run every other test; it also passes on its own in a fresh process.
 """
 import ctypes
 
-import numpy as np
 import pytest
 
 from cases import synthetic_fci
