@@ -351,8 +351,8 @@ class Detset:
 
 
 class RefAlgDetset:
-    """The reference's one-species sigma with its own data structures (hash-map determinant index, linear
-    det_idx_unfold by every thread, per-thread private sigma, critical merge; ref_restated.cpp), for timing the
+    """The reference's sigma builders (one and two species) with its own data structures (hash-map determinant
+    index, linear det_idx_unfold, per-thread private sigma, critical merge; ref_restated.cpp), for timing the
     reference algorithm and for checking it against the oracle."""
 
     def __init__(self, prob: CIProblem):
@@ -370,7 +370,7 @@ class RefAlgDetset:
         self._desc, self._keep = prob.orc_desc()
         self._h = _refalg.refalg_create(ctypes.byref(self._desc))
         if not self._h:
-            raise ValueError("reference restatement: one species only, with complete integral blocks")
+            raise ValueError("reference restatement: one or two species, with complete integral blocks")
         self.n_dets = _refalg.refalg_n_dets(self._h)
 
     def __del__(self):
