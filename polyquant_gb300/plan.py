@@ -1,0 +1,79 @@
+"""Sizing a CI problem before it is built: determinant counts and the device
+memory of the Davidson solver, from the problem definition alone (no GPU).
+
+``count_determinants`` counts the determinant list that create_excitation
+(src/ci/detset/determinant_creation.cpp:148-206) produces: per species and
+spin the strings with k replacements relative to the HF string number
+C(n_e, k) * C(n_orb - n_e, k) for k = 0..ex_max (the reference aborts when
+ex_max exceeds the virtual orbitals, determinant_creation.cpp:54-56, and so
+does this count); a species' (alpha, beta) pair is kept when its total level
+is within the species' total limit, and the levels of all species together
+within max_collective_excitation_level.  (With one species the product
+space is limited by min(total, collective).)
+
+``davidson_device_bytes`` is the device memory the Davidson solver of this
+library allocates for a problem of n_dets determinants: the subspace V and
+its sigma W (n_dets x m_max each), the Ritz vectors, residuals and a work
+block (n_dets x k, n_dets x k, n_dets x max(k, m0)), all FP64, plus the two
+interleaved sigma work vectors (4 per determinant, FP64); m_max follows the
+reference's choice max(2 * num_subspace_vec, 10 * num_states)
+(src/ci/epci.cpp:589-590) unless max_subspace is given.  Handle tables, the
+diagonal (8 B per determinant) and the caller's own vectors come on top.
+"""
+from __future__ import annotations
+
+from math import comb
+from typing import List, Sequence
+
+INT_MAX = 2 ** 31 - 1
+
+
+def string_counts(n_orb: int, n_e: int, ex_max: int) -> List[int]:
+    """Number of strings with exactly k replacements, k = 0..ex_max (reference order groups them by k)."""
+    n_virt = n_orb - n_e
+    out = []
+    for k in range(ex_max + 1):
+        if k > n_virt:
+            raise ValueError(f"excitation level {k} exceeds the {n_virt} virtual orbitals")
+        out.append(comb(n_e, k) * comb(n_virt, k))
+    return out
+
+
+def _pair_levels(n_orb: int, n_alpha: int, n_beta: int, ex: Sequence[int]) -> List[int]:
+    """count[L] of kept (alpha, beta) string pairs with total level L <= ex[2]."""
+    a = string_counts(n_orb, n_alpha, ex[0])
+    b = string_counts(n_orb, n_beta, ex[1])
+    out = [0] * (ex[2] + 1)
+    for ka, na in enumerate(a):
+        for kb, nb in enumerate(b):
+            if ka + kb <= ex[2]:
+                out[ka + kb] += na * nb
+    return out
+
+
+def count_determinants(n_orb: Sequence[int], n_alpha: Sequence[int], n_beta: Sequence[int],
+                       excitation_level: Sequence[Sequence[int]],
+                       max_collective_excitation_level: int = INT_MAX) -> int:
+    """Length of the determinant list of a one- or two-species problem."""
+    ns = len(n_orb)
+    if ns not in (1, 2):
+        raise ValueError("one or two species")
+    mc = max_collective_excitation_level
+    if ns == 1:
+        ex = list(excitation_level[0])
+        ex[2] = min(ex[2], mc)
+        return sum(_pair_levels(n_orb[0], n_alpha[0], n_beta[0], ex)) if ex[2] >= 0 else 0
+    p0 = _pair_levels(n_orb[0], n_alpha[0], n_beta[0], excitation_level[0])
+    p1 = _pair_levels(n_orb[1], n_alpha[1], n_beta[1], excitation_level[1])
+    return sum(c0 * c1 for l0, c0 in enumerate(p0) for l1, c1 in enumerate(p1) if l0 + l1 <= mc)
+
+
+def davidson_device_bytes(n_dets: int, num_states: int, num_subspace_vec: int = 5, max_subspace: int = 0) -> int:
+    """Device bytes of the Davidson work arrays for n_dets determinants (see the module docstring)."""
+    k = num_states
+    m0 = min(max(num_subspace_vec, k), n_dets)
+    m_max = max_subspace if max_subspace > 0 else max(2 * num_subspace_vec, 10 * k)
+    m_max = min(max(m_max, m0 + k), n_dets)
+    vectors = 8 * n_dets * (2 * m_max + 2 * k + max(k, m0))
+    sigma_work = 2 * 8 * 4 * (n_dets + 1)
+    return vectors + sigma_work
