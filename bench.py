@@ -40,12 +40,18 @@ METRIC = "sigma dets/s"
 UNIT = "dets/s"
 
 
-def peaks():
+def _measured_peak(key, fallback):
+    """(value, "measured") from MEASURED_PEAKS.json, or (fallback, "fallback") when the file or key is absent."""
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(path):
-        d = json.load(open(path))
-        return float(d["hbm_gbs"]), "measured"
-    return 6800.0, "fallback"
+    try:
+        with open(path) as f:
+            return float(json.load(f)[key]), "measured"
+    except (OSError, KeyError, TypeError, ValueError):
+        return fallback, "fallback"
+
+
+def peaks():
+    return _measured_peak("hbm_gbs", 6800.0)
 
 
 class ClockSampler:
@@ -173,10 +179,7 @@ def run_reference(args, rank, world):
 
 
 def peak_bf16():
-    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(path):
-        return float(json.load(open(path))["bf16_tflops"]), "measured"
-    return 1900.0, "fallback"
+    return _measured_peak("bf16_tflops", 1900.0)
 
 
 def bench_ao2mo(n=256, L=1024, seed=0):
