@@ -1,8 +1,8 @@
 """Host-side mirror of polyquant's determinant-set operator on the GB300 library.
 
 ``POLYQUANT_DETSET`` keeps the reference's operator interface
-(src/ci/determinant_set.hpp:120-170): ``rows()``, ``cols()``, ``op(i, i)``
-(the diagonal, slater_condon.cpp:5-7), ``op * X`` / ``op @ X`` (sigma,
+(src/ci/determinant_set.hpp:120-170): ``rows()``, ``cols()``, ``op(i, j)`` /
+``Slater_Condon(i, j)`` (any element, slater_condon.cpp:4-100), ``op * X`` / ``op @ X`` (sigma,
 direct.cpp:5-18) and ``create_sigma(sigma, C)`` (direct.cpp:21-33).  Every
 operation calls the C ABI of libpq_gb300.so; there is no CPU path.
 
@@ -134,9 +134,16 @@ class POLYQUANT_DETSET:
         return self._diag
 
     def __call__(self, i: int, j: int) -> float:
-        if i != j:
-            raise NotImplementedError("only diagonal elements are exposed (the Davidson preconditioner needs H_II)")
-        return float(self.diagonal()[i].item())
+        """H_ij, as the reference's operator()(i, j) = Slater_Condon(i, j) (determinant_set.hpp:139): the
+        diagonal from the device diagonal; an off-diagonal element from one FP64 sigma of the unit vector e_j
+        (O(N_dets) work, as the reference's Slater_Condon is through det_idx_unfold)."""
+        if i == j:
+            return float(self.diagonal()[i])
+        e = np.zeros(self.N_dets)
+        e[j] = 1.0
+        return float(self.sigma(e)[i])
+
+    Slater_Condon = __call__
 
     def sigma(self, C, precision: int = PQ_FP64):
         """sigma = H C.  C: torch CUDA tensor (n_dets,) or (n_dets, k) float64, or a numpy array."""

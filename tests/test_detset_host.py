@@ -46,3 +46,19 @@ def test_create_1rdm_argument_order():
     ds.create_1rdm(0, 0, 1, C[:, 1])    # a single vector
     c, spin, species = calls[-1]
     assert torch.equal(c, C[:, 1]) and spin == 1 and species == 0
+
+
+def test_element_access_matches_the_matrix():
+    """operator()(i, j) = Slater_Condon(i, j) (determinant_set.hpp:139): diagonal and off-diagonal elements."""
+    from polyquant_gb300.detset import POLYQUANT_DETSET
+
+    rng = np.random.default_rng(0)
+    H = rng.standard_normal((6, 6))
+    H = H + H.T
+    ds = POLYQUANT_DETSET.__new__(POLYQUANT_DETSET)
+    ds._h, ds.N_dets = None, 6
+    ds.diagonal = lambda: np.diag(H).copy()
+    ds.sigma = lambda C: H @ C
+    for i in range(6):
+        for j in range(6):
+            assert ds(i, j) == H[i, j] and ds.Slater_Condon(i, j) == H[i, j]
