@@ -190,9 +190,24 @@ class POLYQUANT_DETSET:
         return out
 
     def det_unfold(self) -> np.ndarray:
+        """(N_dets, 2 * n_species) string indices of every determinant, in determinant order."""
         out = np.zeros((self.N_dets, 2 * self.n_species), dtype=np.int32)
         check(_lib.load().pq_ci_det_unfold(self._h, out.ctypes.data))
         return out
+
+    def det_idx_unfold(self, det_idx: int):
+        """String indices of one determinant, as the reference's det_idx_unfold (determinant_creation.cpp:378-388),
+        which raises for an index outside the list where the reference aborts."""
+        if not 0 <= det_idx < self.N_dets:
+            raise IndexError(f"det_idx_unfold: {det_idx} outside 0..{self.N_dets - 1}")
+        if getattr(self, "_unfold", None) is None:
+            self._unfold = self.det_unfold()
+        return [int(x) for x in self._unfold[det_idx]]
+
+    def get_det(self, idx_part: int, idx_spin: int, i: int) -> np.ndarray:
+        """Words of string i of a species and spin in the reference layout (word 0 = highest orbitals),
+        as get_det (determinant_creation.cpp:390)."""
+        return self.strings(idx_part, idx_spin)[i]
 
     # ---- eigen-solver ----------------------------------------------------------
     # ---- explicit Hamiltonian (create_ham, explicit_ham.cpp:51-84) -----------

@@ -62,3 +62,16 @@ def test_element_access_matches_the_matrix():
     for i in range(6):
         for j in range(6):
             assert ds(i, j) == H[i, j] and ds.Slater_Condon(i, j) == H[i, j]
+
+
+def test_unfold_and_get_det_mirrors():
+    from polyquant_gb300.detset import POLYQUANT_DETSET
+
+    ds = POLYQUANT_DETSET.__new__(POLYQUANT_DETSET)
+    ds._h, ds.N_dets, ds.n_species = None, 3, 1
+    ds.det_unfold = lambda: np.array([[0, 0], [0, 1], [1, 0]], dtype=np.int32)
+    ds.strings = lambda s, sp: np.array([[0b0011], [0b0101]], dtype=np.uint64)
+    assert ds.det_idx_unfold(2) == [1, 0]
+    with pytest.raises(IndexError):
+        ds.det_idx_unfold(3)
+    assert int(ds.get_det(0, 1, 1)[0]) == 0b0101
