@@ -114,17 +114,34 @@ pq_status pq_ci_sigma_host(pq_ci_handle *h, const double *C, int64_t ldc, int32_
  * array compiled into the library, so n_dets * w * sizeof(T) must not exceed
  * 16 MiB, where w = 4 for nvec >= 3 (else nvec) and T is double (PQ_FP64) or
  * float (PQ_FP32); larger problems return PQ_ERR_ARG.  The array's device
- * address is looked up on the first call on each device (make that call
- * before any stream capture).  All calls share the array: calls that overlap
- * on the GPU race and must be serialised by the caller. */
+ * address is looked up on the first call in each CUDA context (make that call
+ * before any stream capture) and kept for that context; do not use the
+ * library across a cudaDeviceReset, which can move the array.  All calls
+ * share the array: calls that overlap on the GPU race and must be serialised
+ * by the caller. */
 pq_status pq_ci_sigma_noalloc(pq_ci_handle *h, const double *C, int64_t ldc, int32_t nvec, double *S, int64_t lds,
                               int32_t precision);
+
+/* Hamiltonian elements H_IJ = <I|H|J> for any pair of determinant indices
+ * (POLYQUANT_DETSET::operator()(i, j) = Slater_Condon(i, j),
+ * src/ci/determinant_set.hpp:139, src/ci/detset/slater_condon.cpp:4-100).
+ * Exact FP64, computed from the connections of I as sigma applies them, so an
+ * explicit matrix built with a screening threshold does not change them.
+ * pq_ci_elements: I, J, out are HOST arrays of n entries (n <= 2^26); indices
+ * outside 0..n_dets-1 return PQ_ERR_ARG.  Blocking. */
+pq_status pq_ci_element(pq_ci_handle *h, int64_t i, int64_t j, double *out);
+pq_status pq_ci_elements(pq_ci_handle *h, int64_t n, const int64_t *I, const int64_t *J, double *out);
 
 /* Native-layout sigma on DEVICE buffers interleaved by determinant:
  * X[det * nvec + v].  T = double (precision PQ_FP64) or float (PQ_FP32).
  * diag_shift is subtracted from H_II (sigma = (H - shift*1) X). */
 pq_status pq_ci_sigma_interleaved(pq_ci_handle *h, const void *X, void *Y, int32_t nvec, int32_t precision,
                                   double diag_shift);
+
+/* Diagnostic, no reference counterpart: device bytes the handle holds as
+ * grow-on-demand work memory (the interleaved vectors of pq_ci_sigma and the
+ * transposed copies of the FP32 full-CI sigma).  Meant for tests. */
+pq_status pq_debug_scratch_bytes(const pq_ci_handle *h, int64_t *bytes);
 
 /* Block Davidson on the GPU (replaces Spectra::DavidsonSymEigsSolver with the
  * reference's parameters: initial = num_subspace_vec, max = max(2*initial,

@@ -19,7 +19,7 @@ PQ_XFORM_FP64, PQ_XFORM_BF16X3, PQ_XFORM_TF32X3 = 0, 1, 2
 EXPORTS = [
     "pq_last_error", "pq_version", "pq_ci_create", "pq_ci_destroy", "pq_ci_num_dets", "pq_ci_strings",
     "pq_ci_det_unfold", "pq_ci_diag", "pq_ci_sigma", "pq_ci_sigma_host", "pq_ci_sigma_noalloc",
-    "pq_ci_sigma_interleaved",
+    "pq_ci_sigma_interleaved", "pq_ci_element", "pq_ci_elements", "pq_debug_scratch_bytes",
     "pq_ci_davidson", "pq_ci_ham_build", "pq_ci_ham_release", "pq_ci_ham_csr", "pq_ci_s2", "pq_ci_rdm1",
     "pq_ci_batch_create", "pq_ci_batch_destroy", "pq_ci_batch_num_dets", "pq_ci_batch_sigma",
     "pq_ci_batch_tuning", "pq_ci_batch_davidson", "pq_ao2mo", "pq_mo1", "pq_debug_set_wait_budget",
@@ -103,6 +103,12 @@ def load(path: str = LIB_PATH):
     for f in (L.pq_ci_sigma, L.pq_ci_sigma_host, L.pq_ci_sigma_noalloc):
         f.restype = I32
         f.argtypes = [P, P, I64, I32, P, I64, I32]
+    L.pq_ci_element.restype = I32
+    L.pq_ci_element.argtypes = [P, I64, I64, ctypes.POINTER(D)]
+    L.pq_ci_elements.restype = I32
+    L.pq_ci_elements.argtypes = [P, I64, P, P, P]
+    L.pq_debug_scratch_bytes.restype = I32
+    L.pq_debug_scratch_bytes.argtypes = [P, ctypes.POINTER(I64)]
     L.pq_ci_sigma_interleaved.restype = I32
     L.pq_ci_sigma_interleaved.argtypes = [P, P, P, I32, I32, D]
     L.pq_ci_davidson.restype = I32

@@ -189,6 +189,15 @@ pq_status pq_ci_sigma_interleaved(pq_ci_handle *h, const void *X, void *Y, int32
   return ci_sigma_il(h, X, Y, nvec, precision, diag_shift);
 }
 
+pq_status pq_debug_scratch_bytes(const pq_ci_handle *h, int64_t *bytes) {
+  if (!h || !bytes) {
+    set_error("pq_debug_scratch_bytes: NULL argument");
+    return PQ_ERR_ARG;
+  }
+  *bytes = (int64_t)(h->x_il.bytes + h->y_il.bytes + h->x_t.bytes + h->z_t.bytes);
+  return PQ_OK;
+}
+
 pq_status pq_ci_davidson(pq_ci_handle *h, const pq_davidson_params *p, double *energies, double *vecs,
                          pq_davidson_report *report) {
   clear_error();

@@ -15,14 +15,19 @@
 //  * one 4-vector block of the interleaved work vectors must fit 16 MiB:
 //    n_dets * width * sizeof(T) <= 16 MiB (width 1, 2 or 4; T = double or
 //    float), larger problems are rejected with PQ_ERR_ARG;
-//  * the device address of the array is looked up once per device, on the
-//    first call made with that device current; make that first call before
-//    any stream capture;
+//  * the device address of the array is looked up once per CUDA context, on
+//    the first call made in that context; make that first call before any
+//    stream capture.  A cudaDeviceReset destroys the context and can move the
+//    array, so the library must not be used across one;
 //  * all calls share the one array: calls that overlap on the GPU (other
 //    streams or threads) race and must be serialised by the caller.
 // Nothing in the array has to start at zero: each call writes every element
 // of the work vectors it reads (the padding lanes included) before use.
+#include <cuda.h>  // CUcontext (the type only; the driver call is reached through the runtime)
+
 #include <mutex>
+#include <utility>
+#include <vector>
 
 #include "pq_internal.h"
 
@@ -33,28 +38,63 @@ constexpr size_t kNoAllocHalfBytes = size_t(16) << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[2 * kNoAllocHalfBytes];
 
 static std::mutex g_noalloc_mu;
-static void *g_noalloc_addr[128];
+// (context, device address of the array in it): a module, and so the array,
+// is loaded once per context, so the address is cached per context rather
+// than per device ordinal (a driver-API caller may make its own context
+// current on a device whose primary context already loaded the library)
+static std::vector<std::pair<CUcontext, void *>> g_noalloc_addr;
 
-// Device address of the scratch array for the current device (looked up once
-// per device with that device current).
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+
+static pq_status current_context(CUcontext *ctx) {
+  static CtxGetCurrentFn fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || !p || q != cudaDriverEntryPointSuccess) {
+      set_error("pq_ci_sigma_noalloc: cuCtxGetCurrent not available (%s)", cudaGetErrorString(e));
+      return PQ_ERR_CUDA;
+    }
+    fn = (CtxGetCurrentFn)p;
+  }
+  *ctx = nullptr;
+  if (fn(ctx) != CUDA_SUCCESS) {
+    set_error("pq_ci_sigma_noalloc: cuCtxGetCurrent failed");
+    return PQ_ERR_CUDA;
+  }
+  return PQ_OK;
+}
+
+// Device address of the scratch array in the current context (looked up once
+// per context, with that context current).
 static pq_status noalloc_scratch(void **out) {
   int dev = -1;
   PQ_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 128) {
-    set_error("pq_ci_sigma_noalloc: device ordinal %d out of range", dev);
-    return PQ_ERR_STATE;
-  }
+  CUcontext ctx = nullptr;
+  PQ_TRY(current_context(&ctx));
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
-    void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      set_error("pq_ci_sigma_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
-      return PQ_ERR_CUDA;
-    }
-    g_noalloc_addr[dev] = p;
+  if (ctx)
+    for (const auto &e : g_noalloc_addr)
+      if (e.first == ctx) {
+        *out = e.second;
+        return PQ_OK;
+      }
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    set_error("pq_ci_sigma_noalloc: cudaGetSymbolAddress failed on device %d: %s", dev, cudaGetErrorString(e));
+    return PQ_ERR_CUDA;
   }
-  *out = g_noalloc_addr[dev];
+  // with no context current before, the lookup made the device's primary context current
+  if (!ctx) PQ_TRY(current_context(&ctx));
+  for (const auto &c : g_noalloc_addr)
+    if (c.first == ctx) {
+      *out = c.second;
+      return PQ_OK;
+    }
+  g_noalloc_addr.emplace_back(ctx, p);
+  *out = p;
   return PQ_OK;
 }
 

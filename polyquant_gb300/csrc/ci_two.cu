@@ -491,6 +491,52 @@ pq_status ci_ham_rows2(pq_ci_handle *h, double thr, int32_t *cnt, const int64_t 
   return PQ_OK;
 }
 
+// H_IJ for a list of pairs, thread per pair: the diagonal element, or the
+// partner J among the connections of I (the same elements as sigma and the
+// explicit matrix); pairs that are not connected give 0.
+__global__ void elements_two_kernel(Args2<double> p, int64_t n, const int32_t *t4, const int64_t *I, const int64_t *J,
+                                    double *out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t target = J[i];
+  double v = 0.0;
+  if (I[i] == target) {
+    v = p.diag[target];
+  } else {
+    const int t[4] = {t4[4 * i], t4[4 * i + 1], t4[4 * i + 2], t4[4 * i + 3]};
+    uint64_t m[4];
+#pragma unroll
+    for (int s = 0; s < 4; s++) m[s] = p.l[s].str[t[s]];
+    two_conn_visit(p, t, m, [&](int64_t j, double h) {
+      if (j == target) v = h;
+    });
+  }
+  out[i] = v;
+}
+
+pq_status ci_elements2(pq_ci_handle *h, int64_t n, const int32_t *t4, const int64_t *I, const int64_t *J, double *out) {
+  const Args2<double> a = make_args<double>(h);
+  const unsigned grid = (unsigned)((n + 127) / 128);
+  if (grid) elements_two_kernel<<<grid, 128, 0, h->stream>>>(a, n, t4, I, J, out);
+  PQ_CUDA_TRY(cudaGetLastError());
+  return PQ_OK;
+}
+
+// String indices (species-0 alpha, beta, species-1 alpha, beta) of one
+// determinant: the species-0 pair whose block holds I, then its block entry.
+void ci_unfold2_one(const pq_ci_handle *h, int64_t I, int32_t *t) {
+  const int64_t ie = (int64_t)(std::upper_bound(h->ebase.begin(), h->ebase.end(), I) - h->ebase.begin()) - 1;
+  // empty blocks share their successor's base: step back to the block that holds I
+  int64_t k = ie;
+  while (k > 0 && (h->elev[k] < 0 || h->ebase[k] + h->psize[h->elev[k]] <= I)) k--;
+  const int L = h->elev[k];
+  const int64_t q = I - h->ebase[k];
+  t[0] = h->e_a[k];
+  t[1] = h->e_b[k];
+  t[2] = h->pdet_a[h->pfirst[L] + q];
+  t[3] = h->pdet_b[h->pfirst[L] + q];
+}
+
 pq_status ci_unfold2(const pq_ci_handle *h, int32_t *out) {
   int64_t k = 0;
   for (size_t ie = 0; ie < h->e_a.size(); ie++) {

@@ -127,6 +127,10 @@ pq_status build_spin_tables(pq_ci_handle *h, int s, int sp, const double *h1_hos
 pq_status ci_build2(pq_ci_handle *h);
 pq_status ci_sigma2_il(pq_ci_handle *h, const void *X, void *Y, int nvp, int precision, double shift);
 pq_status ci_unfold2(const pq_ci_handle *h, int32_t *out);
+// exact H_IJ of listed pairs: device arrays (t4 = string indices of each I), and the host unfold of one
+// determinant of a two-species space
+pq_status ci_elements2(pq_ci_handle *h, int64_t n, const int32_t *t4, const int64_t *I, const int64_t *J, double *out);
+void ci_unfold2_one(const pq_ci_handle *h, int64_t I, int32_t *t);
 // explicit-H rows of a two-species space: counts when cnt != NULL, else fills col/val at row_ptr
 pq_status ci_ham_rows2(pq_ci_handle *h, double thr, int32_t *cnt, const int64_t *row_ptr, int32_t *col, double *val);
 // ci_sigma.cu
@@ -137,6 +141,8 @@ pq_status ci_sigma_il(pq_ci_handle *h, const void *X, void *Y, int nvec, int pre
 pq_status ci_ham_spmv(pq_ci_handle *h, const void *X, void *Y, int nvp);
 // exact FP64 columns H[:, dets[c]] into column-major W (one species)
 pq_status ci_unit_columns(pq_ci_handle *h, const std::vector<int64_t> &dets, double *W);
+// ci_element.cu: exact H_IJ of n pairs (host index arrays, host output)
+pq_status ci_elements(pq_ci_handle *h, int64_t n, const int64_t *I, const int64_t *J, double *out);
 // ci_sigma32.cu
 bool sigma32_v2_applicable(const pq_ci_handle *h);
 pq_status ci_sigma32_v2(pq_ci_handle *h, const void *X, void *Y, int nvp, double shift);

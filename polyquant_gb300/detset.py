@@ -133,17 +133,38 @@ class POLYQUANT_DETSET:
             self._diag = out
         return self._diag
 
+    def _check_index(self, what: str, k) -> int:
+        if isinstance(k, (bool, np.bool_)) or not isinstance(k, (int, np.integer)):
+            raise TypeError(f"{what}: determinant index must be an integer, got {type(k).__name__}")
+        if not 0 <= int(k) < self.N_dets:
+            raise IndexError(f"{what}: determinant index {int(k)} outside 0..{self.N_dets - 1}")
+        return int(k)
+
     def __call__(self, i: int, j: int) -> float:
-        """H_ij, as the reference's operator()(i, j) = Slater_Condon(i, j) (determinant_set.hpp:139): the
-        diagonal from the device diagonal; an off-diagonal element from one FP64 sigma of the unit vector e_j
-        (O(N_dets) work, as the reference's Slater_Condon is through det_idx_unfold)."""
-        if i == j:
-            return float(self.diagonal()[i])
-        e = np.zeros(self.N_dets)
-        e[j] = 1.0
-        return float(self.sigma(e)[i])
+        """H_ij, as the reference's operator()(i, j) = Slater_Condon(i, j) (determinant_set.hpp:139,
+        slater_condon.cpp:4-100): exact FP64 for any pair, from the connections of determinant i
+        (pq_ci_element), whatever an explicit matrix built with a screening threshold has pruned."""
+        i, j = self._check_index("operator()", i), self._check_index("operator()", j)
+        v = ctypes.c_double()
+        check(_lib.load().pq_ci_element(self._h, i, j, ctypes.byref(v)), "pq_ci_element")
+        return v.value
 
     Slater_Condon = __call__
+
+    def elements(self, I, J) -> np.ndarray:
+        """H_IJ for arrays of index pairs (one library call)."""
+        I = np.ascontiguousarray(np.asarray(I, dtype=np.int64).reshape(-1))
+        J = np.ascontiguousarray(np.asarray(J, dtype=np.int64).reshape(-1))
+        if I.shape != J.shape:
+            raise ValueError("elements: I and J differ in length")
+        bad = (I < 0) | (I >= self.N_dets) | (J < 0) | (J >= self.N_dets)
+        if bad.any():
+            k = int(np.argmax(bad))
+            raise IndexError(f"elements: pair ({I[k]}, {J[k]}) outside 0..{self.N_dets - 1}")
+        out = np.zeros(I.shape[0])
+        check(_lib.load().pq_ci_elements(self._h, I.shape[0], I.ctypes.data, J.ctypes.data, out.ctypes.data),
+              "pq_ci_elements")
+        return out
 
     def sigma(self, C, precision: int = PQ_FP64):
         """sigma = H C.  C: torch CUDA tensor (n_dets,) or (n_dets, k) float64, or a numpy array."""

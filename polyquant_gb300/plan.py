@@ -17,7 +17,11 @@ its sigma W (n_dets x m_max each), the Ritz vectors, residuals and a work
 block (n_dets x k, n_dets x k, n_dets x max(k, m0)), all FP64, plus the two
 interleaved sigma work vectors (4 per determinant, FP64); m_max follows the
 reference's choice max(2 * num_subspace_vec, 10 * num_states)
-(src/ci/epci.cpp:589-590) unless max_subspace is given.  Handle tables, the
+(src/ci/epci.cpp:589-590) unless max_subspace is given.  With
+``precision=PQ_FP32`` (mixed) on a one-species full-CI space the FP32 sigma
+adds its two transposed vector copies (4 FP32 values per determinant each);
+with ``explicit_nnz`` (an explicit matrix built for sigma) the CSR arrays
+(12 B per stored entry plus 8 B per row) are counted too.  Handle tables, the
 diagonal (8 B per determinant) and the caller's own vectors come on top.
 """
 from __future__ import annotations
@@ -68,12 +72,18 @@ def count_determinants(n_orb: Sequence[int], n_alpha: Sequence[int], n_beta: Seq
     return sum(c0 * c1 for l0, c0 in enumerate(p0) for l1, c1 in enumerate(p1) if l0 + l1 <= mc)
 
 
-def davidson_device_bytes(n_dets: int, num_states: int, num_subspace_vec: int = 5, max_subspace: int = 0) -> int:
-    """Device bytes of the Davidson work arrays for n_dets determinants (see the module docstring)."""
+def davidson_device_bytes(n_dets: int, num_states: int, num_subspace_vec: int = 5, max_subspace: int = 0,
+                          precision: int = 0, full_ci: bool = True, explicit_nnz: int = 0) -> int:
+    """Device bytes of the Davidson work arrays for n_dets determinants (see the module docstring).
+    precision: 0 = FP64, 1 = mixed (FP32 sigma with FP64 refinement); full_ci: one-species space with every
+    (alpha, beta) pair (the FP32 sigma then keeps transposed copies); explicit_nnz: stored entries of an
+    explicit matrix that sigma multiplies with (0: none)."""
     k = num_states
     m0 = min(max(num_subspace_vec, k), n_dets)
     m_max = max_subspace if max_subspace > 0 else max(2 * num_subspace_vec, 10 * k)
     m_max = min(max(m_max, m0 + k), n_dets)
     vectors = 8 * n_dets * (2 * m_max + 2 * k + max(k, m0))
     sigma_work = 2 * 8 * 4 * (n_dets + 1)
-    return vectors + sigma_work
+    fp32_transposed = 2 * 4 * 4 * (n_dets + 1) if precision == 1 and full_ci else 0
+    csr = (12 * explicit_nnz + 8 * (n_dets + 1)) if explicit_nnz > 0 else 0
+    return vectors + sigma_work + fp32_transposed + csr

@@ -21,8 +21,9 @@ the datasets of the /MultiDet group:
   nstate                   max over species of active + frozen orbitals
 
 ``multidet_payload`` returns them as numpy arrays keyed by dataset name;
-``write_multidet`` stores them under /MultiDet of an HDF5 file with h5py, or
-in an .npz archive with the same keys where h5py is not installed.
+``write_multidet`` stores them under /MultiDet of an HDF5 file with h5py.  The
+HDF5 format itself is not written here: without h5py the call raises, unless
+the caller asks for an .npz archive with the same keys (``allow_npz=True``).
 """
 from __future__ import annotations
 
@@ -92,12 +93,16 @@ def _masks(words: np.ndarray) -> np.ndarray:
     return w[:, -1] if w.ndim == 2 else w
 
 
-def write_multidet(path: str, payload: Dict[str, np.ndarray]) -> str:
-    """Store the payload under /MultiDet of the HDF5 file ``path`` (h5py), or as ``path`` + '.npz' without h5py.
+def write_multidet(path: str, payload: Dict[str, np.ndarray], allow_npz: bool = False) -> str:
+    """Store the payload under /MultiDet of the HDF5 file ``path`` (needs h5py).  Without h5py this raises
+    RuntimeError, or, with ``allow_npz=True``, writes ``path`` + '.npz' with the same dataset names.
     Returns the file written."""
     try:
         import h5py
     except ImportError:
+        if not allow_npz:
+            raise RuntimeError("write_multidet: writing the QMCPACK HDF5 file needs h5py, which is not installed; "
+                               "pass allow_npz=True to store the /MultiDet datasets as an .npz archive instead")
         out = path + ".npz"
         np.savez(out, **payload)
         return out

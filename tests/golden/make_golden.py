@@ -1,8 +1,8 @@
 """Regenerate the golden fixtures of tests/golden/ from the reference's own test data.
 
-Run once in a checkout that has the polyquant sources at $POLYQUANT_REF
-(default /root/reference); the npz files are committed so that the tests never
-read the reference tree at run time.
+Run once with the environment variable POLYQUANT_REF set to the root of a
+polyquant source checkout (the directory holding tests/data/); the npz files
+are committed so that the tests never read the reference tree at run time.
 
 Sources (paths inside the polyquant project):
   h2o_sto3g_golden.npz
@@ -25,7 +25,7 @@ import os
 
 import numpy as np
 
-REF = os.environ.get("POLYQUANT_REF", "/root/reference")
+REF = os.environ.get("POLYQUANT_REF", "")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -92,6 +92,8 @@ def positron_bases():
 
 
 if __name__ == "__main__":
+    if not REF or not os.path.isdir(os.path.join(REF, "tests", "data")):
+        raise SystemExit("set POLYQUANT_REF to the root of a polyquant source checkout (with tests/data/)")
     h2o()
     h_minus()
     positron_bases()

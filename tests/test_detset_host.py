@@ -48,20 +48,24 @@ def test_create_1rdm_argument_order():
     assert torch.equal(c, C[:, 1]) and spin == 1 and species == 0
 
 
-def test_element_access_matches_the_matrix():
-    """operator()(i, j) = Slater_Condon(i, j) (determinant_set.hpp:139): diagonal and off-diagonal elements."""
+def test_element_access_checks_indices_before_the_library():
+    """operator()(i, j) = Slater_Condon(i, j) (determinant_set.hpp:139) takes determinant indices
+    0..N_dets-1: a negative or too large index, or a non-integer, raises before any library call."""
     from polyquant_gb300.detset import POLYQUANT_DETSET
 
-    rng = np.random.default_rng(0)
-    H = rng.standard_normal((6, 6))
-    H = H + H.T
     ds = POLYQUANT_DETSET.__new__(POLYQUANT_DETSET)
     ds._h, ds.N_dets = None, 6
-    ds.diagonal = lambda: np.diag(H).copy()
-    ds.sigma = lambda C: H @ C
-    for i in range(6):
-        for j in range(6):
-            assert ds(i, j) == H[i, j] and ds.Slater_Condon(i, j) == H[i, j]
+    for i, j in ((-1, 0), (0, -1), (6, 0), (0, 6), (2 ** 40, 1)):
+        with pytest.raises(IndexError):
+            ds(i, j)
+        with pytest.raises(IndexError):
+            ds.Slater_Condon(i, j)
+    with pytest.raises(TypeError):
+        ds(1.0, 2)
+    with pytest.raises(IndexError):
+        ds.elements([0, 1, 6], [0, 1, 2])
+    with pytest.raises(ValueError):
+        ds.elements([0, 1], [0])
 
 
 def test_unfold_and_get_det_mirrors():

@@ -38,3 +38,8 @@ def test_davidson_bytes():
     b = davidson_device_bytes(n, 4, 20)
     assert b == 8 * n * (2 * 40 + 2 * 4 + 20) + 2 * 8 * 4 * (n + 1)
     assert davidson_device_bytes(10, 2, 5, max_subspace=50) == 8 * 10 * (2 * 10 + 4 + 5) + 64 * 11
+    # mixed precision on full CI adds the FP32 sigma's two transposed copies; an explicit matrix its CSR
+    base = davidson_device_bytes(n, 4, 20)
+    assert davidson_device_bytes(n, 4, 20, precision=1) == base + 2 * 16 * (n + 1)
+    assert davidson_device_bytes(n, 4, 20, precision=1, full_ci=False) == base
+    assert davidson_device_bytes(100, 2, 5, explicit_nnz=1000) == davidson_device_bytes(100, 2, 5) + 12000 + 808

@@ -36,6 +36,40 @@ def _run(L, fn, g, C, prec):
     return st, S
 
 
+def _scratch_bytes(L, g):
+    b = ctypes.c_int64(-1)
+    assert L.pq_debug_scratch_bytes(g._h, ctypes.byref(b)) == 0
+    return b.value
+
+
+@pytest.mark.parametrize("prec_name", ["fp64", "fp32"])
+def test_noalloc_on_a_fresh_handle_grows_no_handle_memory(prec_name):
+    """The entry point's promise: on a handle that never ran pq_ci_sigma, calls leave the handle's
+    grow-on-demand work buffers (interleaved vectors, transposed FP32 copies) at zero bytes; the results
+    still agree with pq_ci_sigma, which is run afterwards and does grow them."""
+    from polyquant_gb300 import _lib
+
+    L = _lib.load()
+    prec, rtol = (_lib.PQ_FP64, SIGMA_RTOL_FP64) if prec_name == "fp64" else (_lib.PQ_FP32, SIGMA_RTOL_FP32)
+    # full CI, so that FP32 pq_ci_sigma would take the transposing path with its extra buffers
+    g = _detset(synthetic_fci(9, 4, 4, seed=45))
+    assert _scratch_bytes(L, g) == 0
+    gen = torch.Generator(device="cuda").manual_seed(11)
+    outs = []
+    for k in (4, 2, 4):
+        C = torch.randn(k, g.N_dets, device="cuda", dtype=torch.float64, generator=gen)
+        st, S = _run(L, L.pq_ci_sigma_noalloc, g, C, prec)
+        assert st == _lib.PQ_OK, _lib.last_error()
+        assert _scratch_bytes(L, g) == 0
+        outs.append((C, S))
+    for C, S in outs:
+        st_ref, S_ref = _run(L, L.pq_ci_sigma, g, C, prec)
+        assert st_ref == _lib.PQ_OK
+        assert (S - S_ref).abs().max().item() <= rtol * S_ref.abs().max().item()
+    assert _scratch_bytes(L, g) > 0
+    g.close()
+
+
 def test_noalloc_matches_pq_ci_sigma_on_consecutive_calls():
     from polyquant_gb300 import _lib
 
