@@ -194,7 +194,8 @@ pq_status pq_debug_scratch_bytes(const pq_ci_handle *h, int64_t *bytes) {
     set_error("pq_debug_scratch_bytes: NULL argument");
     return PQ_ERR_ARG;
   }
-  *bytes = (int64_t)(h->x_il.bytes + h->y_il.bytes + h->x_t.bytes + h->z_t.bytes);
+  *bytes = (int64_t)(h->x_il.bytes + h->y_il.bytes + h->x_t.bytes + h->z_t.bytes + h->tc_xp.bytes + h->tc_zp.bytes +
+                     h->tc_btab.bytes + h->tc_aux.bytes);
   return PQ_OK;
 }
 

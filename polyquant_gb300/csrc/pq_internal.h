@@ -100,6 +100,13 @@ struct pq_ci_handle {
   // scratch of the FP32 full-CI sigma (transposed copies) and the transposed cross block
   pq::DevBuf x_t, z_t, d_eba32;
   bool fp32_v2 = false;  // FP32 sigma uses ci_sigma32.cu
+  // FP32 alpha-beta doubles on the tensor cores (ci_sigma32_tc.cu): planar vector copies, beta scatter
+  // table, scale of the integrals, error word and max |X|
+  pq::DevBuf tc_xp, tc_zp, tc_btab, tc_aux;
+  float tc_sw = 1.0f;
+  int tc_sms = 0;
+  bool tc_ready = false;
+  bool fp32_tc = false;  // the FP32 full-CI sigma uses the tensor-core alpha-beta path
   // two species: addressing of the product space (see ci_two.cu)
   std::vector<int32_t> e_a, e_b;        // species-0 (alpha, beta) string pair of each kept pair ie
   std::vector<int64_t> ebase;           // first determinant of pair ie's species-1 block
@@ -146,6 +153,9 @@ pq_status ci_elements(pq_ci_handle *h, int64_t n, const int64_t *I, const int64_
 // ci_sigma32.cu
 bool sigma32_v2_applicable(const pq_ci_handle *h);
 pq_status ci_sigma32_v2(pq_ci_handle *h, const void *X, void *Y, int nvp, double shift);
+// ci_sigma32_tc.cu: Y += alpha-beta doubles of X (FP32, interleaved), on the tensor cores
+bool sigma32_tc_applicable(const pq_ci_handle *h);
+pq_status ci_sigma32_ab_tc(pq_ci_handle *h, const void *X, void *Y, int nvp);
 pq_status ci_to_il(pq_ci_handle *h, const double *C, int64_t ldc, int v0, int nv, int nvp, int precision, void *X);
 pq_status ci_from_il(pq_ci_handle *h, const void *Y, int v0, int nv, int nvp, int precision, double *S, int64_t lds);
 // ci_davidson.cu

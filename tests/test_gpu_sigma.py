@@ -147,6 +147,41 @@ def test_sigma_fp32_full_ci_medium():
         assert (S32 - S64).abs().max().item() <= SIGMA_RTOL_FP32 * S64.abs().max().item()
 
 
+@pytest.mark.parametrize("shape", [(10, 5, 4), (13, 6, 6), (7, 3, 3), (9, 1, 4)])
+def test_sigma_fp32_tensor_core_alpha_beta_matches_scatter_path(monkeypatch, shape):
+    """The FP32 full-CI sigma with its alpha-beta doubles on the tensor cores (FP16 hi/lo split, FP32
+    accumulation) against the same sigma with the FP32 vector-atomic scatter (PQ_SIGMA32_NO_TC, read when a
+    handle is created) and against FP64, for beta rows that fill 1 to 14 column tiles (the last one partial),
+    fewer alpha singles than the GEMM's K = 64, and widths 1, 2, 4."""
+    from polyquant_gb300._lib import PQ_FP32
+
+    n, a, b = shape
+    p = synthetic_fci(n, a, b, seed=30 + n)
+    g_tc = gpu_detset(p)
+    monkeypatch.setenv("PQ_SIGMA32_NO_TC", "1")
+    g_sc = gpu_detset(p)
+    monkeypatch.delenv("PQ_SIGMA32_NO_TC")
+    gen = torch.Generator(device="cuda").manual_seed(n)
+    for k in (1, 2, 4, 3):
+        X = torch.randn(g_tc.N_dets, k, device="cuda", dtype=torch.float64, generator=gen)
+        S64 = g_tc.sigma(X)
+        S_tc = g_tc.sigma(X, precision=PQ_FP32)
+        S_sc = g_sc.sigma(X, precision=PQ_FP32)
+        scale = S64.abs().max().item()
+        assert (S_tc - S64).abs().max().item() <= SIGMA_RTOL_FP32 * scale
+        assert (S_sc - S64).abs().max().item() <= SIGMA_RTOL_FP32 * scale
+        # the scaled split keeps 22 bits: no worse than FP32 arithmetic by more than a small factor
+        assert (S_tc - S64).abs().max().item() <= 10 * max((S_sc - S64).abs().max().item(), 1e-7 * scale)
+    # tiny and large magnitudes: the power-of-two scaling keeps the relative accuracy
+    for f in (1e-30, 1e20):
+        X = f * torch.randn(g_tc.N_dets, 2, device="cuda", dtype=torch.float64, generator=gen)
+        S64 = g_tc.sigma(X)
+        S_tc = g_tc.sigma(X, precision=PQ_FP32)
+        assert (S_tc - S64).abs().max().item() <= SIGMA_RTOL_FP32 * S64.abs().max().item()
+    g_tc.close()
+    g_sc.close()
+
+
 def test_davidson_h2o_energies(cases, h2o):
     """H2O/STO-3G CISD energies (calculation_test.cpp:253-260) and FCI vs the oracle's dense H."""
     r = h2o("library")
