@@ -1,7 +1,9 @@
 """Build libpq_gb300.so (all CUDA/C++ sources of the package) for sm_103a with nvcc.
 
 The library is built in-tree into ``polyquant_gb300/lib/``; object files go to
-``polyquant_gb300/_build/``.  Translation units compile in parallel.
+``polyquant_gb300/_build/``.  Translation units compile in parallel.  Extra nvcc
+flags (for instance a diagnostic define) come from the environment variable
+PQ_NVCC_EXTRA; objects are rebuilt when forced.
 """
 from __future__ import annotations
 
@@ -42,7 +44,7 @@ def _compile(src: str, verbose_ptxas: bool) -> str:
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), _deps()):
         return obj
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-I", os.path.join(ROOT, "include"),
-           "-I", CSRC, "-c", src, "-o", obj + ".tmp"]
+           "-I", CSRC, "-c", src, "-o", obj + ".tmp", *os.environ.get("PQ_NVCC_EXTRA", "").split()]
     if verbose_ptxas and src.endswith(".cu"):
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -165,16 +165,27 @@ pq_status pq_ci_sigma_host(pq_ci_handle *h, const double *C, int64_t ldc, int32_
     return PQ_ERR_ARG;
   }
   int64_t n = h->n_dets;
-  DevBuf dc, ds;
-  PQ_TRY(dc.alloc(sizeof(double) * (size_t)n * nvec + 16));
-  PQ_TRY(ds.alloc(sizeof(double) * (size_t)n * nvec + 16));
-  for (int v = 0; v < nvec; v++)
-    PQ_CUDA_TRY(cudaMemcpyAsync(dc.as<double>() + (size_t)v * n, C + (size_t)v * ldc, sizeof(double) * n,
-                                cudaMemcpyHostToDevice, h->stream));
-  PQ_TRY(sigma_device(h, dc.as<double>(), n, nvec, ds.as<double>(), n, precision));
-  for (int v = 0; v < nvec; v++)
-    PQ_CUDA_TRY(cudaMemcpyAsync(S + (size_t)v * lds, ds.as<double>() + (size_t)v * n, sizeof(double) * n,
-                                cudaMemcpyDeviceToHost, h->stream));
+  // device copies of C and sigma stay with the handle (grow-only), so repeated calls allocate nothing;
+  // with ldc == n (and lds == n) each block moves in one copy
+  const size_t bytes = sizeof(double) * (size_t)n * nvec + 16;
+  PQ_TRY(h->host_c.ensure(bytes));
+  PQ_TRY(h->host_s.ensure(bytes));
+  double *dc = h->host_c.as<double>(), *ds = h->host_s.as<double>();
+  if (ldc == n) {
+    PQ_CUDA_TRY(cudaMemcpyAsync(dc, C, sizeof(double) * (size_t)n * nvec, cudaMemcpyHostToDevice, h->stream));
+  } else {
+    for (int v = 0; v < nvec; v++)
+      PQ_CUDA_TRY(cudaMemcpyAsync(dc + (size_t)v * n, C + (size_t)v * ldc, sizeof(double) * n, cudaMemcpyHostToDevice,
+                                  h->stream));
+  }
+  PQ_TRY(sigma_device(h, dc, n, nvec, ds, n, precision));
+  if (lds == n) {
+    PQ_CUDA_TRY(cudaMemcpyAsync(S, ds, sizeof(double) * (size_t)n * nvec, cudaMemcpyDeviceToHost, h->stream));
+  } else {
+    for (int v = 0; v < nvec; v++)
+      PQ_CUDA_TRY(cudaMemcpyAsync(S + (size_t)v * lds, ds + (size_t)v * n, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                                  h->stream));
+  }
   PQ_CUDA_TRY(cudaStreamSynchronize(h->stream));
   return PQ_OK;
 }
@@ -194,8 +205,8 @@ pq_status pq_debug_scratch_bytes(const pq_ci_handle *h, int64_t *bytes) {
     set_error("pq_debug_scratch_bytes: NULL argument");
     return PQ_ERR_ARG;
   }
-  *bytes = (int64_t)(h->x_il.bytes + h->y_il.bytes + h->x_t.bytes + h->z_t.bytes + h->tc_xp.bytes + h->tc_zp.bytes +
-                     h->tc_btab.bytes + h->tc_aux.bytes);
+  *bytes = (int64_t)(h->x_il.bytes + h->y_il.bytes + h->x_t.bytes + h->z_t.bytes + h->tc_btab.bytes + h->tc_aux.bytes +
+                     h->host_c.bytes + h->host_s.bytes);
   return PQ_OK;
 }
 
