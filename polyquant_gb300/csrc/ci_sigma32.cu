@@ -10,9 +10,9 @@
 //      (Ja, Ib) of a warp are consecutive in memory.
 //   2. beta-side terms (beta singles, beta-beta doubles): the same kernel on the
 //      transposed copy XT[b][a], result transposed back and added.
-//   3. alpha-beta doubles: for up to 16 orbitals and 64 alpha singles per
-//      string, a GEMM per alpha string on the tcgen05 tensor cores
-//      (ci_sigma32_tc.cu).  Otherwise input-stationary on the CUDA cores: CTA
+//   3. alpha-beta doubles: for blocks of four vectors, up to 16 orbitals and
+//      64 alpha singles per string, a GEMM per alpha string on the tcgen05
+//      tensor cores (ci_sigma32_tc.cu).  Otherwise input-stationary on the CUDA cores: CTA
 //      per alpha string Ja, lane per alpha single (Ja -> Ia_i).  For each beta
 //      string Ib the warp loads the vectors C(Ja, Jb) of Ib's beta singles once
 //      (one broadcast load each) and every lane applies its own coefficient
@@ -315,7 +315,7 @@ static pq_status sigma32_v2_impl(pq_ci_handle *h, const float *X, float *Y, doub
   PQ_CUDA_TRY(cudaGetLastError());
   // 5. alpha-beta doubles: on the tensor cores where the shape allows (ci_sigma32_tc.cu), else
   // scattered with vector atomics
-  if (h->fp32_tc) return ci_sigma32_ab_tc(h, X, Y, NV);
+  if (h->fp32_tc && NV == 4) return ci_sigma32_ab_tc(h, X, Y, NV);
   ABArgs b{};
   const SpinTablesDev &ta = h->tab[0][0], &tbb = h->tab[0][1];
   b.a_off = ta.s1_off.as<int64_t>();

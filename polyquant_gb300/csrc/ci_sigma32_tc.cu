@@ -5,83 +5,112 @@
 // element of same_part_ham_double (slater_condon_singleparticle.cpp:107-175):
 //   sigma(Ia, Ib) += sum_{a in singles(Ia)} sum_{b in singles(Ib)}
 //                    s_a s_b (pair_a | pair_b) C(Ja(a), Jb(b)).
-// Written as a GEMM per (alpha string Ia, root v):
-//   D[Jb][q] = sum_a X_v[Ja(a)][Jb] * s_a (pair_a | q)      (q: off-diagonal beta pairs)
-//   sigma(Ia, Ib) += s_b D[Jb(b)][q(b)]  for every beta single b of Ib,
+// Written as a GEMM per alpha string Ia over the interleaved vectors
+// X[Ja][Jb][v] of four roots (the roots ride along the M dimension):
+//   D[(Jb, v)][q] = sum_a X[Ja(a)][Jb][v] * s_a (pair_a | q)      (q: off-diagonal beta pairs)
+//   sigma(Ia, Ib, v) += s_b D[(Jb(b), v)][q(b)]  for every beta single b of Ib,
 // i.e. for every column Jb, each off-diagonal pair q that moves Jb to a string
-// Ib scatters D[Jb][q] with the single's phase into the sigma row of Ia.
+// Ib adds D[(Jb, .)][q] with the single's phase into sigma(Ia, Ib, .).
 //
-// Kernel: persistent, one CTA per SM, alpha strings assigned round-robin; the
-// roots of one alpha string share its B operand.  Warp roles:
-//   warp 0      TMA producer: one 512-byte bulk copy per alpha single per
-//               128-column tile of the planar vector X_v (rows Ja(a));
-//   warp 1      TMEM owner and MMA issuer (M = 128 columns Jb, N = 128 pairs,
-//               K = 64 singles; hi*hi + hi*lo + lo*hi in FP16 with FP32
+// Kernel: persistent, one CTA per SM, alpha strings assigned round-robin.  Warp roles:
+//   warp 0      TMEM owner and MMA issuer (M = 128 rows (Jb, v), N = 128
+//               pairs, K = 64 singles; hi*hi + hi*lo + lo*hi in FP16 with FP32
 //               accumulation; two accumulators so the epilogue overlaps);
-//   warps 2-5   converters: scaled FP32 rows -> FP16 hi/lo in the K-major
-//               128-byte-swizzled operand layout; they also build B per alpha
-//               string from the cross-spin integrals;
-//   warps 6-9   epilogue: tcgen05.ld of the accumulator, scatter through the
-//               [pair][Jb] table into the sigma row in shared memory; at the
-//               end of an item the row is written (scaled back) to Z_v[Ia].
+//   warps 1-4   converters, thread <-> operand row: each thread copies its own
+//               column of the 64 gathered rows of a 128-value tile into a
+//               shared stage with 4-byte asynchronous copies, one tile ahead,
+//               then scales it, splits it into FP16 hi/lo and writes the
+//               K-major 128-byte-swizzled operand tile (two stages); they also
+//               build B per alpha string from the cross-spin integrals (two
+//               buffers, so the next string's B is ready before its tiles);
+//   warps 5-8   epilogue: tcgen05.ld of the accumulator; per 32-column chunk a
+//               warp parks its values in its own shared block and reads them
+//               back so that each lane holds the four roots of one (Jb, q),
+//               then adds them to sigma(Ia, target) with one vector reduction
+//               (red.global.add.v4.f32); the [Jb][q] scatter-table rows of the
+//               next tile arrive in shared memory by asynchronous copies while
+//               the MMAs run.
+// A CTA is the only writer of its sigma rows, so the reductions never contend
+// between CTAs.  On this GPU a shared-memory float atomic adds fewer values
+// per clock than a global vector reduction, which carries all four roots.
 // Scaling: X and the integrals are multiplied by powers of two that bring
 // their largest magnitudes to [2^14, 2^15) (FP16 range, exact in FP32), and
-// the result by the inverse.  The split x = hi + lo with hi, lo in FP16 keeps
+// the result by the inverses.  The split x = hi + lo with hi, lo in FP16 keeps
 // 22 significant bits; the three products are exact in FP32.
 // Every mbarrier wait is bounded; a wait that runs out records an error code,
 // sets an abort flag that every role polls, and the kernel winds down (the
-// producer waits, bounded, for its own copies, the MMA thread for its own
-// MMAs, TMEM is freed); the host reports PQ_TIMEOUT.
+// MMA thread waits, bounded, for its own MMAs, TMEM is freed); the host
+// reports PQ_TIMEOUT.
 #include <cuda_fp16.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 
 #include "pq_internal.h"
 
 namespace pq {
 namespace abtc {
 
-constexpr int BM = 128;       // beta columns per tile (TMEM lanes)
+constexpr int BM = 128;       // (Jb, v) rows per tile (TMEM lanes)
 constexpr int BN = 128;       // off-diagonal beta pairs (TMEM columns per accumulator)
 constexpr int BK = 64;        // alpha singles (K), one 128-byte swizzle span of FP16
-constexpr int STAGES = 2;
+constexpr int NV = 4;         // roots per determinant (interleaved); other widths use the CUDA-core path
+constexpr int ASTAGES = 2;    // A operand stages
 constexpr int OP_TILE = BM * BK * 2;          // 16 KB: one FP16 operand tile (A or B)
-constexpr int RAW_TILE = BK * BM * 4;         // 32 KB: the FP32 rows of one tile
-constexpr int NTHREADS = 320;                 // 10 warps
-constexpr int CONV0 = 2, EPI0 = 6;            // first converter / epilogue warp
+constexpr int RAW_TILE = BK * BM * 4;         // 32 KB: the gathered FP32 rows of one tile
+constexpr int WROWS = BM / NV / 4;            // beta strings per epilogue warp and tile (8)
+// scatter-table row in shared memory (uint16): 272 bytes, a multiple of the 16-byte copies that fill it, and
+// 68 words apart so the eight rows a warp reads fall in different banks
+constexpr int TROW = 136;
+constexpr int TAB_STAGE = 4 * WROWS * TROW * 2;  // bytes: one tile's table rows (32 beta strings), 8.5 KB
+constexpr int STG_WARP = WROWS * 32 * NV;        // floats: one warp's 8 beta strings x 32 columns x 4 roots
+constexpr int NTHREADS = 288;                    // 9 warps
+constexpr int CONV0 = 1, EPI0 = 5;               // first converter / epilogue warp
 constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
-constexpr int MAX_ROW = 12928;                // sigma row floats held in shared memory (n_beta <= this)
-// shared memory: A hi/lo x STAGES, B hi/lo, raw x STAGES, sigma row, barriers
-constexpr int SMEM_OPS = STAGES * 2 * OP_TILE + 2 * OP_TILE + STAGES * RAW_TILE;
-constexpr int SMEM_BYTES = SMEM_OPS + MAX_ROW * 4 + 1024 + 256;
+// shared memory: A hi/lo x ASTAGES, B hi/lo x 2, raw rows x 2, table rows x 2, epilogue staging x 4 warps,
+// per-warp alpha partner lists, barriers
+constexpr int SMEM_OPS = ASTAGES * 2 * OP_TILE + 2 * 2 * OP_TILE + 2 * RAW_TILE + 2 * TAB_STAGE + 4 * STG_WARP * 4;
+constexpr int NBARS = 2 * ASTAGES + 9;           // a_full, a_empty, acc_full/empty, b_full/empty, drain
+constexpr int SMEM_BYTES = SMEM_OPS + 4 * BK * 2 + 1024 + NBARS * 8 + 16;
+static_assert((TROW * 2) % 16 == 0 && TAB_STAGE % 16 == 0 && (WROWS * TROW * 2) % 16 == 0,
+              "16-byte copies into the table stage need 16-byte aligned rows");
+static_assert((2 * RAW_TILE + 2 * TAB_STAGE) % 16 == 0, "the epilogue staging is read as float4");
+static_assert(SMEM_BYTES <= 232448, "shared memory per CTA");
 
-enum { ERR_RAW = 1, ERR_AEMPTY = 2, ERR_AFULL = 3, ERR_ACC = 4, ERR_B = 5 };
+enum { ERR_AEMPTY = 2, ERR_AFULL = 3, ERR_ACC = 4, ERR_B = 5 };
 
 struct Args {
-  const float *Xp;         // [v][na][nbp] planar input (FP32)
-  float *Zp;               // [v][na][nbp] planar output
-  const float *xmax;       // max |X| over the input (device scalar, written by the layout pass)
-  int64_t na, nb, nbp;
-  int nvp;
-  int m_tiles;             // nbp / BM
+  const float *X;          // [na][nb][NV] interleaved input (FP32)
+  float *Y;                // [na][nb][NV] interleaved output, added to
+  const float *xmax;       // max |X| over the input (device scalar, written by the reduction pass)
+  int64_t na, nb;
+  int m_tiles;             // ceil(nb * NV / BM)
   const int64_t *a_off;
   const int32_t *a_J, *a_info;
   const float *eab;        // (pair_alpha | pair_beta) row-major FP32
   int npair, n_off;        // beta pairs: all, off-diagonal (<= BN)
   float sw;                // power-of-two scale of the integrals
-  const uint16_t *btab;    // [q][nb]: (Ib << 1 | phase) of the single of Jb through pair q, or 0xFFFF
+  const uint16_t *btab;    // [nb][BN]: (Ib << 1 | phase) of the single of Jb through pair q, or 0xFFFF
   long long wait_cycles;
   int *err;
+  long long *prof;         // per-CTA role timers (PQ_ABTC_PROFILE builds only)
 };
+
+// Role timers (only in builds with PQ_ABTC_PROFILE defined): cycles per slot, summed over a CTA's work and
+// written by one thread of each role at the end.
+#ifdef PQ_ABTC_PROFILE
+#define PT(v) const long long v = clock64()
+#define PACC(slot, v) prof_[slot] += clock64() - (v)
+#else
+#define PT(v)
+#define PACC(slot, v)
+#endif
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
@@ -103,7 +132,6 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long lo
   }
   return true;
 }
-
 // warp-uniform bounded wait: every lane polls; the warp agrees on success only if every lane saw the phase
 __device__ __forceinline__ bool warp_wait(uint32_t bar, uint32_t parity, long long budget) {
   const bool ok = mbar_wait(bar, parity, budget);
@@ -111,12 +139,15 @@ __device__ __forceinline__ bool warp_wait(uint32_t bar, uint32_t parity, long lo
 }
 __device__ __forceinline__ bool warp_aborted(volatile int *flag) { return __any_sync(0xffffffffu, *flag != 0); }
 
-// one-dimensional bulk copy global -> shared, completion counted on `bar` (16-byte aligned, size % 16 == 0)
-__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(src), "r"(bytes), "r"(bar)
-               : "memory");
+// 4-byte / 16-byte asynchronous copies global -> shared (each thread waits for its own groups)
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
 }
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 // UMMA shared-memory descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
@@ -156,15 +187,22 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
-// x = hi + lo with hi, lo in FP16 (x already scaled into FP16 range)
-__device__ __forceinline__ void split_h(float x, __half &h, __half &l) {
-  h = __float2half_rn(x);
-  l = __float2half_rn(x - __half2float(h));
-}
-
-// 8 consecutive K values of row r -> one 16-byte chunk c of the 128-byte-swizzled K-major tile
-__device__ __forceinline__ void store_chunk(unsigned char *tile, int r, int c, const __half (&v)[8]) {
-  *reinterpret_cast<uint4 *>(tile + r * 128 + ((c ^ (r & 7)) << 4)) = *reinterpret_cast<const uint4 *>(v);
+// K values of row r of an operand tile (scaled FP32) -> FP16 hi/lo tiles in the 128-byte-swizzled K-major
+// layout (16-byte chunk c of row r at chunk position c ^ (r & 7)); pairs convert with one packed instruction
+__device__ __forceinline__ void store_row(unsigned char *th, unsigned char *tl, int r, const float (&x)[BK]) {
+#pragma unroll
+  for (int c = 0; c < BK / 8; c++) {
+    __half2 h[4], l[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const float a = x[c * 8 + 2 * e], b = x[c * 8 + 2 * e + 1];
+      h[e] = __floats2half2_rn(a, b);
+      const float2 f = __half22float2(h[e]);
+      l[e] = __floats2half2_rn(a - f.x, b - f.y);
+    }
+    *reinterpret_cast<uint4 *>(th + r * 128 + ((c ^ (r & 7)) << 4)) = *reinterpret_cast<const uint4 *>(h);
+    *reinterpret_cast<uint4 *>(tl + r * 128 + ((c ^ (r & 7)) << 4)) = *reinterpret_cast<const uint4 *>(l);
+  }
 }
 
 // power of two 2^e with x * 2^e in [2^14, 2^15) (1 for x == 0)
@@ -178,35 +216,41 @@ __device__ __forceinline__ float fp16_scale(float x) {
 __global__ void __launch_bounds__(NTHREADS, 1) ab_tc_kernel(Args g) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
-  unsigned char *a_hi = smem;                                   // [STAGES] x 16 KB
-  unsigned char *a_lo = a_hi + STAGES * OP_TILE;                // [STAGES] x 16 KB
-  unsigned char *b_hi = a_lo + STAGES * OP_TILE;                // 16 KB
-  unsigned char *b_lo = b_hi + OP_TILE;                         // 16 KB
-  float *raw = reinterpret_cast<float *>(b_lo + OP_TILE);       // [STAGES][BK][BM]
-  float *srow = raw + STAGES * BK * BM;                         // [MAX_ROW]
-  uint64_t *bars = reinterpret_cast<uint64_t *>(srow + MAX_ROW);
-  uint64_t *raw_full = bars, *raw_empty = bars + 2, *a_full = bars + 4, *a_empty = bars + 6;
-  uint64_t *acc_full = bars + 8, *acc_empty = bars + 10, *b_full = bars + 12, *b_empty = bars + 13, *drain = bars + 14;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 15);
+  unsigned char *a_hi = smem;                                       // [ASTAGES] x 16 KB
+  unsigned char *a_lo = a_hi + ASTAGES * OP_TILE;                   // [ASTAGES] x 16 KB
+  unsigned char *b_hi = a_lo + ASTAGES * OP_TILE;                   // [2] x 16 KB
+  unsigned char *b_lo = b_hi + 2 * OP_TILE;                         // [2] x 16 KB
+  float *raw = reinterpret_cast<float *>(b_lo + 2 * OP_TILE);       // [2][BK][BM]
+  uint16_t *tab = reinterpret_cast<uint16_t *>(raw + 2 * BK * BM);  // [2][4 warps][WROWS][TROW]
+  float *stg_all = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(tab) + 2 * TAB_STAGE);  // [4][STG_WARP]
+  uint16_t *ja_all = reinterpret_cast<uint16_t *>(stg_all + 4 * STG_WARP);  // [4][BK] alpha partner strings
+  uint64_t *bars = reinterpret_cast<uint64_t *>(ja_all + 4 * BK);
+  uint64_t *a_full = bars, *a_empty = bars + ASTAGES, *acc_full = bars + 2 * ASTAGES;
+  uint64_t *acc_empty = acc_full + 2, *b_full = acc_full + 4, *b_empty = acc_full + 6, *drain = acc_full + 8;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#ifdef PQ_ABTC_PROFILE
+  long long prof_[16] = {0};
+  const long long prof_start = clock64();
+#endif
   if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES; s++) {
-      mbar_init(smem_u32(raw_full + s), 1);
-      mbar_init(smem_u32(raw_empty + s), 4);
+    for (int s = 0; s < ASTAGES; s++) {
       mbar_init(smem_u32(a_full + s), 4);
       mbar_init(smem_u32(a_empty + s), 1);
+    }
+    for (int s = 0; s < 2; s++) {
       mbar_init(smem_u32(acc_full + s), 1);
       mbar_init(smem_u32(acc_empty + s), 4);
+      mbar_init(smem_u32(b_full + s), 4);
+      mbar_init(smem_u32(b_empty + s), 1);
     }
-    mbar_init(smem_u32(b_full), 4);
-    mbar_init(smem_u32(b_empty), 1);
     mbar_init(smem_u32(drain), 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 1) {
+  if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                  "r"(2 * BN)
                  : "memory");
@@ -216,252 +260,270 @@ __global__ void __launch_bounds__(NTHREADS, 1) ab_tc_kernel(Args g) {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
   const int mt = g.m_tiles;
+  const int64_t row_len = g.nb * NV;  // floats in one alpha row of X and Y
 
   if (warp == 0) {
-    // ---- producer: 512-byte rows of X_v, one per alpha single, per tile
-    int seq = 0;
-    bool stop = false;
-    for (int64_t ia = blockIdx.x; ia < g.na && !stop; ia += gridDim.x) {
-      const int64_t base = g.a_off[ia];
-      const int n1 = (int)(g.a_off[ia + 1] - base);
-      const int ja0 = lane < n1 ? g.a_J[base + lane] : 0;
-      const int ja1 = lane + 32 < n1 ? g.a_J[base + lane + 32] : 0;
-      for (int v = 0; v < g.nvp && !stop; v++) {
-        const float *xv = g.Xp + (int64_t)v * g.na * g.nbp;
-        for (int t = 0; t < mt; t++) {
-          const int s = seq & 1;
-          const uint32_t ph = (uint32_t)((seq >> 1) & 1);
-          if (!warp_wait(smem_u32(raw_empty + s), ph ^ 1u, g.wait_cycles)) {
-            if (lane == 0) atomicCAS(g.err, 0, ERR_RAW);
-            *abort_flag = 1;
-            stop = true;
-            break;
-          }
-          if (warp_aborted(abort_flag)) {
-            stop = true;
-            break;
-          }
-          const uint32_t bar = smem_u32(raw_full + s);
-          if (lane == 0) mbar_expect_tx(bar, (uint32_t)(n1 * BM * 4));
-          __syncwarp();
-          float *dst = raw + s * BK * BM;
-          const int64_t col = (int64_t)t * BM;
-          if (lane < n1) bulk_load(smem_u32(dst + lane * BM), xv + ja0 * g.nbp + col, BM * 4, bar);
-          if (lane + 32 < n1) bulk_load(smem_u32(dst + (lane + 32) * BM), xv + ja1 * g.nbp + col, BM * 4, bar);
-          seq++;
-        }
-      }
-    }
-    // the copies of the last stages must have landed before the CTA exits
-    if (lane == 0)
-      for (int j = seq > STAGES ? seq - STAGES : 0; j < seq; j++)
-        mbar_wait(smem_u32(raw_full + (j & 1)), (uint32_t)((j >> 1) & 1), WAIT_CYCLES);
-    __syncwarp();
-  } else if (warp == 1) {
     // ---- MMA issuer
     if (lane == 0) {
       int seq = 0, grp = 0;
       bool ok = true;
       for (int64_t ia = blockIdx.x; ia < g.na && ok && !*abort_flag; ia += gridDim.x, grp++) {
-        if (!mbar_wait(smem_u32(b_full), (uint32_t)(grp & 1), g.wait_cycles)) {
+        const int bb = grp & 1;
+        PT(tb0);
+        if (!mbar_wait(smem_u32(b_full + bb), (uint32_t)((grp >> 1) & 1), g.wait_cycles)) {
           atomicCAS(g.err, 0, ERR_B);
-          *abort_flag = 1;
+          ok = false;
           break;
         }
-        for (int v = 0; v < g.nvp && ok; v++) {
-          for (int t = 0; t < mt; t++, seq++) {
-            const int s = seq & 1, a = seq & 1;
-            const uint32_t ph = (uint32_t)((seq >> 1) & 1);
-            if (!mbar_wait(smem_u32(acc_empty + a), ph ^ 1u, g.wait_cycles)) {
-              atomicCAS(g.err, 0, ERR_ACC);
-              ok = false;
-              break;
-            }
-            if (!mbar_wait(smem_u32(a_full + s), ph, g.wait_cycles)) {
-              atomicCAS(g.err, 0, ERR_AFULL);
-              ok = false;
-              break;
-            }
-            if (*abort_flag) {
-              ok = false;
-              break;
-            }
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t d = tmem + (uint32_t)(a * BN);
-            const uint32_t ah = smem_u32(a_hi + s * OP_TILE), al = smem_u32(a_lo + s * OP_TILE);
-            const uint32_t bh = smem_u32(b_hi), bl = smem_u32(b_lo);
-#pragma unroll
-            for (int kk = 0; kk < BK / 16; kk++) {
-              const uint32_t off = kk * 32;  // 16 FP16 values along K
-              mma_f16(d, smem_desc(ah + off), smem_desc(bh + off), kk > 0 ? 1u : 0u);
-              mma_f16(d, smem_desc(ah + off), smem_desc(bl + off), 1u);
-              mma_f16(d, smem_desc(al + off), smem_desc(bh + off), 1u);
-            }
-            mma_commit(smem_u32(a_empty + s));
-            mma_commit(smem_u32(acc_full + a));
+        PACC(3, tb0);
+        const uint32_t bh = smem_u32(b_hi + bb * OP_TILE), bl = smem_u32(b_lo + bb * OP_TILE);
+        for (int t = 0; t < mt; t++, seq++) {
+          const int s = seq % ASTAGES, a = seq & 1;
+          const uint32_t ps = (uint32_t)((seq / ASTAGES) & 1), pa = (uint32_t)((seq >> 1) & 1);
+          PT(tw0);
+          if (!mbar_wait(smem_u32(acc_empty + a), pa ^ 1u, g.wait_cycles)) {
+            atomicCAS(g.err, 0, ERR_ACC);
+            ok = false;
+            break;
           }
+          PACC(1, tw0);
+          PT(tw1);
+          if (!mbar_wait(smem_u32(a_full + s), ps, g.wait_cycles)) {
+            atomicCAS(g.err, 0, ERR_AFULL);
+            ok = false;
+            break;
+          }
+          PACC(2, tw1);
+          if (*abort_flag) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t d = tmem + (uint32_t)(a * BN);
+          const uint32_t ah = smem_u32(a_hi + s * OP_TILE), al = smem_u32(a_lo + s * OP_TILE);
+#pragma unroll
+          for (int kk = 0; kk < BK / 16; kk++) {
+            const uint32_t off = kk * 32;  // 16 FP16 values along K
+            mma_f16(d, smem_desc(ah + off), smem_desc(bh + off), kk > 0 ? 1u : 0u);
+            mma_f16(d, smem_desc(ah + off), smem_desc(bl + off), 1u);
+            mma_f16(d, smem_desc(al + off), smem_desc(bh + off), 1u);
+          }
+          mma_commit(smem_u32(a_empty + s));
+          mma_commit(smem_u32(acc_full + a));
         }
-        if (!ok) {
-          *abort_flag = 1;
-          break;
-        }
-        mma_commit(smem_u32(b_empty));  // B of this alpha string is free once its MMAs completed
+        if (!ok) break;
+        mma_commit(smem_u32(b_empty + bb));  // B of this alpha string is free once its MMAs completed
       }
+      if (!ok) *abort_flag = 1;
       // every MMA issued here has completed before TMEM is freed
       mma_commit(smem_u32(drain));
       mbar_wait(smem_u32(drain), 0, WAIT_CYCLES);
     }
     __syncwarp();
   } else if (warp < EPI0) {
-    // ---- converters: B per alpha string, A per tile; thread <-> operand row
-    const int r = threadIdx.x - 32 * CONV0;  // 0..127
+    // ---- converters: thread <-> operand row (A: element e of the tile, B: off-diagonal beta pair)
+    const int r = threadIdx.x - 32 * CONV0;     // 0..127
+    uint16_t *ja = ja_all + (warp - CONV0) * BK;  // this warp's copy of the alpha partner list
+    const float sx = fp16_scale(*g.xmax);
     int seq = 0, grp = 0;
     bool stop = false;
+    int i = 1;
+    while ((i + 1) * i / 2 <= r) i++;  // off-diagonal pair r = i(i-1)/2 + j, j < i
+    const int qfull = r + i;           // its idx2(i, j) = i(i+1)/2 + j
+    const bool qv = r < g.n_off;
     for (int64_t ia = blockIdx.x; ia < g.na && !stop; ia += gridDim.x, grp++) {
       const int64_t base = g.a_off[ia];
       const int n1 = (int)(g.a_off[ia + 1] - base);
-      if (!warp_wait(smem_u32(b_empty), (uint32_t)(grp & 1) ^ 1u, g.wait_cycles)) {
+      ja[lane] = (uint16_t)(lane < n1 ? g.a_J[base + lane] : 0);
+      ja[lane + 32] = (uint16_t)(lane + 32 < n1 ? g.a_J[base + lane + 32] : 0);
+      __syncwarp();
+      const int bb = grp & 1;
+      PT(cb0);
+      if (!warp_wait(smem_u32(b_empty + bb), (uint32_t)((grp >> 1) & 1) ^ 1u, g.wait_cycles)) {
         if (lane == 0) atomicCAS(g.err, 0, ERR_B);
         *abort_flag = 1;
         break;
       }
       if (warp_aborted(abort_flag)) break;
+      PACC(5, cb0);
+      PT(cb1);
       {
         // B[q][k] = s_k (pair_k | q) * sw for the off-diagonal beta pair q = r
-        int i = 1;
-        while ((i + 1) * i / 2 <= r) i++;  // r = i(i-1)/2 + j with j < i
-        const int qfull = r + i;           // idx2(i, j) = i(i+1)/2 + j
-        const bool qv = r < g.n_off;
-        for (int c = 0; c < BK / 8; c++) {
-          __half h[8], l[8];
+        float w[BK];
 #pragma unroll
-          for (int e = 0; e < 8; e++) {
-            const int k = c * 8 + e;
-            float w = 0.0f;
-            if (qv && k < n1) {
-              const int info = __ldg(g.a_info + base + k);
-              w = __ldg(g.eab + (int64_t)(info >> 1) * g.npair + qfull) * g.sw;
-              if (info & 1) w = -w;
-            }
-            split_h(w, h[e], l[e]);
+        for (int k = 0; k < BK; k++) {
+          w[k] = 0.0f;
+          if (qv && k < n1) {
+            const int info = __ldg(g.a_info + base + k);
+            const float x = __ldg(g.eab + (int64_t)(info >> 1) * g.npair + qfull) * g.sw;
+            w[k] = (info & 1) ? -x : x;
           }
-          store_chunk(b_hi, r, c, h);
-          store_chunk(b_lo, r, c, l);
         }
+        store_row(b_hi + bb * OP_TILE, b_lo + bb * OP_TILE, r, w);
       }
+      PACC(6, cb1);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncwarp();
-      if (lane == 0) mbar_arrive(smem_u32(b_full));
-      const float sx = fp16_scale(*g.xmax);
-      for (int v = 0; v < g.nvp && !stop; v++) {
-        for (int t = 0; t < mt; t++) {
-          const int s = seq & 1;
-          const uint32_t ph = (uint32_t)((seq >> 1) & 1);
-          bool ok = warp_wait(smem_u32(raw_full + s), ph, g.wait_cycles);
-          if (ok) ok = warp_wait(smem_u32(a_empty + s), ph ^ 1u, g.wait_cycles);
-          if (!ok) {
-            if (lane == 0) atomicCAS(g.err, 0, ERR_AEMPTY);
-            *abort_flag = 1;
-            stop = true;
-            break;
-          }
-          if (warp_aborted(abort_flag)) {
-            stop = true;
-            break;
-          }
-          const float *src = raw + s * BK * BM;
-          unsigned char *th = a_hi + s * OP_TILE, *tl = a_lo + s * OP_TILE;
-          for (int c = 0; c < BK / 8; c++) {
-            __half h[8], l[8];
-#pragma unroll
-            for (int e = 0; e < 8; e++) {
-              const int k = c * 8 + e;
-              const float x = k < n1 ? src[k * BM + r] * sx : 0.0f;
-              split_h(x, h[e], l[e]);
-            }
-            store_chunk(th, r, c, h);
-            store_chunk(tl, r, c, l);
-          }
-          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-          __syncwarp();
-          if (lane == 0) {
-            mbar_arrive(smem_u32(a_full + s));
-            mbar_arrive(smem_u32(raw_empty + s));
-          }
-          seq++;
+      if (lane == 0) mbar_arrive(smem_u32(b_full + bb));
+      // A tiles: each thread copies its own column of the 64 gathered rows into the raw stage with 4-byte
+      // asynchronous copies, one tile ahead, and converts only what it copied (no cross-thread wait)
+      auto issue = [&](int t, int stage) {
+        const int64_t e = (int64_t)t * BM + r;
+        if (e < row_len) {
+          const float *col = g.X + e;
+          const uint32_t dst = smem_u32(raw + stage * BK * BM + r);
+          for (int k = 0; k < n1; k++) cp_async4(dst + k * BM * 4, col + (int64_t)ja[k] * row_len);
         }
+        cp_commit();
+      };
+      issue(0, seq & 1);
+      for (int t = 0; t < mt; t++) {
+        PT(cl0);
+        if (t + 1 < mt)
+          issue(t + 1, (seq + 1) & 1);
+        else
+          cp_commit();  // an empty group keeps one group per tile
+        PACC(10, cl0);
+        const int s = seq % ASTAGES;
+        const uint32_t ps = (uint32_t)((seq / ASTAGES) & 1);
+        PT(ca0);
+        if (!warp_wait(smem_u32(a_empty + s), ps ^ 1u, g.wait_cycles)) {
+          if (lane == 0) atomicCAS(g.err, 0, ERR_AEMPTY);
+          *abort_flag = 1;
+          stop = true;
+          break;
+        }
+        if (warp_aborted(abort_flag)) {
+          stop = true;
+          break;
+        }
+        PACC(7, ca0);
+        PT(cc0);
+        cp_wait<1>();  // this tile's copies have landed (the next tile's may still be in flight)
+        PACC(9, cc0);
+        PT(cs0);
+        {
+          const bool in = (int64_t)t * BM + r < row_len;
+          const float *src = raw + (seq & 1) * BK * BM + r;
+          float x[BK];
+#pragma unroll
+          for (int k = 0; k < BK; k++) x[k] = (in && k < n1) ? src[k * BM] * sx : 0.0f;
+          store_row(a_hi + s * OP_TILE, a_lo + s * OP_TILE, r, x);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(a_full + s));
+        PACC(8, cs0);
+        seq++;
       }
+      cp_wait<0>();
+      __syncwarp();
     }
   } else {
-    // ---- epilogue: accumulator -> scatter into the sigma row -> Z_v[ia].  The four epilogue warps meet at
-    // named barriers, so none of them leaves the loop early: after an abort they skip the work but keep
-    // the same sequence of barriers.
-    const int q = warp & 3;                  // TMEM lane quadrant of this warp
-    const int et = threadIdx.x - 32 * EPI0;  // 0..127
+    // ---- epilogue: accumulator -> vector reductions into sigma(Ia, target, 0..3).  Each warp stages and
+    // reads back only its own 32 TMEM lanes (8 beta strings x 4 roots), so the warps never wait on each other.
+    const int q = warp & 3;  // TMEM lane quadrant of this warp
     int seq = 0;
     bool dead = false;
-    for (int i = et; i < MAX_ROW; i += 128) srow[i] = 0.0f;
-    asm volatile("bar.sync 1, 128;" ::: "memory");
-    const float inv = 1.0f / (fp16_scale(*g.xmax) * g.sw);
-    for (int64_t ia = blockIdx.x; ia < g.na; ia += gridDim.x) {
-      for (int v = 0; v < g.nvp; v++) {
-        for (int t = 0; t < mt; t++, seq++) {
-          if (dead) continue;
-          const int a = seq & 1;
-          const uint32_t ph = (uint32_t)((seq >> 1) & 1);
-          if (!warp_wait(smem_u32(acc_full + a), ph, g.wait_cycles)) {
-            if (lane == 0) atomicCAS(g.err, 0, ERR_ACC);
-            *abort_flag = 1;
-            dead = true;
-            continue;
-          }
-          if (warp_aborted(abort_flag)) {
-            dead = true;
-            continue;
-          }
-          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          const int64_t jb = (int64_t)t * BM + q * 32 + lane;
-          const bool live = jb < g.nb;
-          const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * BN);
-#pragma unroll 1
-          for (int c0 = 0; c0 < BN; c0 += 32) {
-            float d[32];
-            tmem_ld32(taddr + c0, d);
-            if (live && c0 < g.n_off) {
-              const uint16_t *tb = g.btab + (int64_t)c0 * g.nb + jb;
+    // the two inverse scales are powers of two inside the FP32 range, and so is their product
+    const float unscale = (1.0f / g.sw) * (1.0f / fp16_scale(*g.xmax));
+    uint16_t *my_tab = tab + q * WROWS * TROW;  // this warp's 8 rows inside a table stage
+    float *stg = stg_all + q * STG_WARP;
+    // scatter-table rows of this warp's 8 beta strings of tile t -> table stage (16-byte copies, 4 per lane)
+    auto issue = [&](int t, int stage) {
+      const int64_t jb0 = ((int64_t)t * BM + q * 32) / NV;  // first beta string of this warp's rows
+      const uint32_t base = smem_u32(my_tab + stage * (TAB_STAGE / 2));
 #pragma unroll
-              for (int j = 0; j < 32; j++) {
-                const uint16_t e = __ldg(tb + (int64_t)j * g.nb);
-                if (e != 0xFFFFu) atomicAdd(srow + (e >> 1), (e & 1) ? -d[j] : d[j]);
-              }
+      for (int i = 0; i < 4; i++) {
+        const int piece = lane + 32 * i;  // 8 rows x 16 pieces of 16 bytes
+        const int row = piece >> 4, pc = piece & 15;
+        if ((jb0 + row) * NV < row_len) cp_async16(base + row * TROW * 2 + pc * 16, g.btab + (jb0 + row) * BN + pc * 8);
+      }
+      cp_commit();
+    };
+    issue(0, seq & 1);
+    for (int64_t ia = blockIdx.x; ia < g.na; ia += gridDim.x) {
+      float *yrow = g.Y + ia * row_len;
+      for (int t = 0; t < mt; t++, seq++) {
+        if (dead) continue;
+        issue(t + 1 < mt ? t + 1 : 0, (seq + 1) & 1);  // the next tile's rows load while this tile waits
+        const int a = seq & 1;
+        const uint32_t pa = (uint32_t)((seq >> 1) & 1);
+        PT(ew0);
+        if (!warp_wait(smem_u32(acc_full + a), pa, g.wait_cycles)) {
+          if (lane == 0) atomicCAS(g.err, 0, ERR_ACC);
+          *abort_flag = 1;
+          dead = true;
+          continue;
+        }
+        if (warp_aborted(abort_flag)) {
+          dead = true;
+          continue;
+        }
+        cp_wait<1>();
+        __syncwarp();
+        PACC(11, ew0);
+        PT(es0);
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * BN);
+        // per 32-column chunk: lane (row rr = lane / 4, root vv = lane % 4) parks its values in the warp's
+        // staging block (column swizzled by the row: conflict-free), then lane c takes column c of each of
+        // the warp's 8 beta strings with its four roots and adds them with one vector reduction
+        const int64_t jb0 = ((int64_t)t * BM + q * 32) / NV;
+        const int rr = lane / NV, vv = lane % NV;
+        const uint16_t *trow = my_tab + (seq & 1) * (TAB_STAGE / 2);
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 32) {
+          float d[32];
+          tmem_ld32(taddr + c0, d);
+#pragma unroll
+          for (int j = 0; j < 32; j++) stg[(rr * 32 + (j ^ rr)) * NV + vv] = d[j];
+          __syncwarp();
+#pragma unroll
+          for (int i = 0; i < WROWS; i++) {
+            const bool live = (jb0 + i) * NV < row_len;
+            const uint32_t en = live ? trow[i * TROW + c0 + lane] : 0xFFFFu;
+            if (en != 0xFFFFu) {
+              const float4 x = *reinterpret_cast<const float4 *>(stg + (i * 32 + (lane ^ i)) * NV);
+              const float f = (en & 1) ? -unscale : unscale;
+              asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(yrow + (int64_t)(en >> 1) * NV),
+                           "f"(x.x * f), "f"(x.y * f), "f"(x.z * f), "f"(x.w * f)
+                           : "memory");
             }
           }
-          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
           __syncwarp();
-          if (lane == 0) mbar_arrive(smem_u32(acc_empty + a));
         }
-        asm volatile("bar.sync 1, 128;" ::: "memory");
-        float *z = g.Zp + ((int64_t)v * g.na + ia) * g.nbp;
-        for (int i = et; i < g.nbp; i += 128) {
-          if (!dead) z[i] = srow[i] * inv;
-          srow[i] = 0.0f;
-        }
-        asm volatile("bar.sync 1, 128;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(acc_empty + a));
+        PACC(12, es0);
       }
     }
+    cp_wait<0>();
   }
+#ifdef PQ_ABTC_PROFILE
+  {
+    const long long tot = clock64() - prof_start;
+    long long *o = g.prof + blockIdx.x * 16;
+    if (threadIdx.x == 0) {
+      o[0] = tot;
+      for (int i = 1; i <= 3; i++) o[i] = prof_[i];
+    }
+    if (threadIdx.x == 32 * CONV0) {
+      o[4] = tot;
+      for (int i = 5; i <= 10; i++) o[i] = prof_[i];
+    }
+    if (threadIdx.x == 32 * EPI0)
+      for (int i = 11; i <= 12; i++) o[i] = prof_[i];
+  }
+#endif
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN) : "memory");
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN) : "memory");
 }
 
-}  // namespace abtc
-}  // namespace pq
-
-namespace pq {
-namespace abtc {
-
-// btab[q][Jb] for every beta single of Jb: q = off-diagonal index of its pair, entry (Ib << 1 | phase)
+// btab[Jb][q] for every beta single of Jb: q = off-diagonal index of its pair (row length BN), entry
+// (Ib << 1 | phase); every other entry stays 0xFFFF
 __global__ void btab_kernel(const int64_t *off, const int32_t *J, const int32_t *info, int64_t nb, uint16_t *btab) {
   const int64_t jb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (jb >= nb) return;
@@ -470,60 +532,38 @@ __global__ void btab_kernel(const int64_t *off, const int32_t *J, const int32_t 
     int i = 1;
     while ((i + 1) * (i + 2) / 2 <= pr) i++;  // largest i with i(i+1)/2 <= pr
     const int q = pr - i;                     // i(i-1)/2 + j
-    btab[(int64_t)q * nb + jb] = (uint16_t)(((uint32_t)J[e] << 1) | (uint32_t)(info[e] & 1));
+    btab[jb * BN + q] = (uint16_t)(((uint32_t)J[e] << 1) | (uint32_t)(info[e] & 1));
   }
 }
 
-// Xp[v][a][b] = X[(a * nb + b) * NV + v] (rows padded to nbp; the padding is left as it is), and
 // xmax = max |X| (as the bit pattern of a non-negative float, so integer max orders it)
-template <int NV>
-__global__ void to_planar_kernel(const float *X, int64_t na, int64_t nb, int64_t nbp, float *Xp, unsigned *xmax) {
+__global__ void absmax_kernel(const float *X, int64_t n, unsigned *xmax) {
   float m = 0.0f;
-  const int64_t n = na * nb;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t a = i / nb, b = i - a * nb;
-#pragma unroll
-    for (int v = 0; v < NV; v++) {
-      const float x = X[i * NV + v];
-      Xp[((int64_t)v * na + a) * nbp + b] = x;
-      m = fmaxf(m, fabsf(x));
-    }
-  }
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(X[i]));
   for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) atomicMax(xmax, __float_as_uint(m));
-}
-
-// Y[(a * nb + b) * NV + v] += Zp[v][a][b]
-template <int NV>
-__global__ void planar_add_kernel(const float *Zp, int64_t na, int64_t nb, int64_t nbp, float *Y) {
-  const int64_t n = na * nb;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t a = i / nb, b = i - a * nb;
-#pragma unroll
-    for (int v = 0; v < NV; v++) Y[i * NV + v] += Zp[((int64_t)v * na + a) * nbp + b];
-  }
 }
 
 }  // namespace abtc
 
 // The tensor-core alpha-beta path applies to one-species full CI with at most
 // 16 orbitals (the 120 off-diagonal beta pairs fit N = 128), at most 64 alpha
-// singles per string (K = 64) and a beta row that fits shared memory.
+// singles per string (K = 64), fewer than 32768 beta strings (16-bit targets
+// in the scatter table) and fewer than 65536 alpha strings (16-bit partner
+// lists).
 bool sigma32_tc_applicable(const pq_ci_handle *h) {
   if (h->n_species != 1 || !h->full) return false;
   const int n = h->n_orb[0];
   if (n > 16 || n * (n - 1) / 2 > abtc::BN) return false;
   if (h->tab[0][0].max1 > abtc::BK) return false;
-  const int64_t nb = h->tab[0][1].n_str;
-  return nb <= abtc::MAX_ROW && nb < 32768;
+  return h->tab[0][1].n_str < 32768 && h->tab[0][0].n_str < 65536;
 }
 
-template <int NV>
 static pq_status ab_tc_impl(pq_ci_handle *h, const float *X, float *Y) {
   using namespace abtc;
   cudaStream_t st = h->stream;
   const int64_t na = h->tab[0][0].n_str, nb = h->tab[0][1].n_str;
-  const int64_t nbp = (nb + BM - 1) / BM * BM;
   const int n = h->n_orb[0], npair = h->npair[0];
   if (!h->tc_ready) {
     // one-off: the beta scatter table, the integral scale, the kernel's shared-memory limit
@@ -548,27 +588,19 @@ static pq_status ab_tc_impl(pq_ci_handle *h, const float *X, float *Y) {
     PQ_CUDA_TRY(cudaDeviceGetAttribute(&h->tc_sms, cudaDevAttrMultiProcessorCount, dev));
     h->tc_ready = true;
   }
-  const size_t planar = sizeof(float) * (size_t)NV * na * nbp;
-  if (h->tc_xp.bytes < planar) {
-    PQ_TRY(h->tc_xp.alloc(planar));
-    PQ_CUDA_TRY(cudaMemsetAsync(h->tc_xp.ptr, 0, planar, st));  // the row padding stays zero
-  }
-  PQ_TRY(h->tc_zp.ensure(planar));
   unsigned *xmax = h->tc_aux.as<unsigned>();
   int *err = reinterpret_cast<int *>(xmax + 1);
   PQ_CUDA_TRY(cudaMemsetAsync(h->tc_aux.ptr, 0, 8, st));
-  const unsigned g = (unsigned)std::min<int64_t>((na * nb + 255) / 256, 152 * 16);
-  to_planar_kernel<NV><<<g, 256, 0, st>>>(X, na, nb, nbp, h->tc_xp.as<float>(), xmax);
+  const int64_t len = na * nb * NV;
+  absmax_kernel<<<(unsigned)std::min<int64_t>((len + 255) / 256, 152 * 8), 256, 0, st>>>(X, len, xmax);
   PQ_CUDA_TRY(cudaGetLastError());
   Args a{};
-  a.Xp = h->tc_xp.as<float>();
-  a.Zp = h->tc_zp.as<float>();
+  a.X = X;
+  a.Y = Y;
   a.xmax = reinterpret_cast<const float *>(xmax);
   a.na = na;
   a.nb = nb;
-  a.nbp = nbp;
-  a.nvp = NV;
-  a.m_tiles = (int)(nbp / BM);
+  a.m_tiles = (int)((nb * NV + BM - 1) / BM);
   const SpinTablesDev &ta = h->tab[0][0];
   a.a_off = ta.s1_off.as<int64_t>();
   a.a_J = ta.s1_J.as<int32_t>();
@@ -580,6 +612,12 @@ static pq_status ab_tc_impl(pq_ci_handle *h, const float *X, float *Y) {
   a.btab = h->tc_btab.as<uint16_t>();
   a.wait_cycles = WAIT_CYCLES;
   a.err = err;
+#ifdef PQ_ABTC_PROFILE
+  DevBuf prof;
+  PQ_TRY(prof.alloc(sizeof(long long) * 16 * 1024));
+  PQ_CUDA_TRY(cudaMemsetAsync(prof.ptr, 0, sizeof(long long) * 16 * 1024, st));
+  a.prof = prof.as<long long>();
+#endif
   const unsigned grid = (unsigned)std::min<int64_t>(na, h->tc_sms > 0 ? h->tc_sms : 148);
   ab_tc_kernel<<<grid, NTHREADS, SMEM_BYTES, st>>>(a);
   PQ_CUDA_TRY(cudaGetLastError());
@@ -590,16 +628,26 @@ static pq_status ab_tc_impl(pq_ci_handle *h, const float *X, float *Y) {
     set_error("sigma32 alpha-beta tensor-core kernel: a pipeline wait ran out (code %d)", herr);
     return PQ_TIMEOUT;
   }
-  planar_add_kernel<NV><<<g, 256, 0, st>>>(h->tc_zp.as<float>(), na, nb, nbp, Y);
-  PQ_CUDA_TRY(cudaGetLastError());
+#ifdef PQ_ABTC_PROFILE
+  {
+    std::vector<long long> pr((size_t)16 * grid);
+    PQ_CUDA_TRY(cudaMemcpy(pr.data(), prof.ptr, sizeof(long long) * pr.size(), cudaMemcpyDeviceToHost));
+    const char *names[13] = {"total", "mma:wait_acc_empty", "mma:wait_a_full", "mma:wait_b_full", "conv:total",
+                             "conv:wait_b_empty", "conv:b_build", "conv:wait_a_empty", "conv:convert_store",
+                             "conv:wait_copies", "conv:issue_copies", "epi:wait_acc_full", "epi:scatter"};
+    for (int i = 0; i < 13; i++) {
+      double m = 0;
+      for (unsigned b = 0; b < grid; b++) m += (double)pr[16 * b + i];
+      fprintf(stderr, "abtc-prof %-22s %14.0f cycles/CTA\n", names[i], m / grid);
+    }
+  }
+#endif
   return PQ_OK;
 }
 
 pq_status ci_sigma32_ab_tc(pq_ci_handle *h, const void *X, void *Y, int nvp) {
-  if (nvp == 1) return ab_tc_impl<1>(h, (const float *)X, (float *)Y);
-  if (nvp == 2) return ab_tc_impl<2>(h, (const float *)X, (float *)Y);
-  if (nvp == 4) return ab_tc_impl<4>(h, (const float *)X, (float *)Y);
-  set_error("sigma32 tensor-core path: unsupported width %d", nvp);
+  if (nvp == abtc::NV) return ab_tc_impl(h, (const float *)X, (float *)Y);
+  set_error("sigma32 tensor-core path: width %d (the path takes %d vectors)", nvp, abtc::NV);
   return PQ_ERR_ARG;
 }
 

@@ -97,12 +97,14 @@ struct pq_ci_handle {
   pq::DevBuf d_diag;
   // scratch for layout conversion
   pq::DevBuf x_il, y_il;
+  // device staging of pq_ci_sigma_host (column-major C and sigma)
+  pq::DevBuf host_c, host_s;
   // scratch of the FP32 full-CI sigma (transposed copies) and the transposed cross block
   pq::DevBuf x_t, z_t, d_eba32;
   bool fp32_v2 = false;  // FP32 sigma uses ci_sigma32.cu
-  // FP32 alpha-beta doubles on the tensor cores (ci_sigma32_tc.cu): planar vector copies, beta scatter
-  // table, scale of the integrals, error word and max |X|
-  pq::DevBuf tc_xp, tc_zp, tc_btab, tc_aux;
+  // FP32 alpha-beta doubles on the tensor cores (ci_sigma32_tc.cu): beta scatter table, scale of the
+  // integrals, error word and max |X|
+  pq::DevBuf tc_btab, tc_aux;
   float tc_sw = 1.0f;
   int tc_sms = 0;
   bool tc_ready = false;
