@@ -59,9 +59,13 @@ template <typename T> struct Args2 {
   double shift;
   const T *X;
   T *Y;
+  // full product of complete string spaces: det(t) = ((t0 * nst[1] + t1) * nst[2] + t2) * nst[3] + t3
+  int nst[4];
 };
 
-template <typename T> __device__ __forceinline__ int64_t lookup2(const Args2<T> &p, const int (&t)[4]) {
+template <typename T, bool FULL = false>
+__device__ __forceinline__ int64_t lookup2(const Args2<T> &p, const int (&t)[4]) {
+  if (FULL) return (((int64_t)t[0] * p.nst[1] + t[1]) * p.nst[2] + t[2]) * p.nst[3] + t[3];
   if (t[1] >= p.rowlen0[t[0]]) return -1;
   const int ie = p.rowoff0[t[0]] + t[1];
   const int L = p.elev[ie];
@@ -102,7 +106,8 @@ template <typename T> __device__ __forceinline__ T coul_col(const T *M, int ld, 
 // Coulomb terms, alpha-beta doubles within a species, single x single cross
 // doubles, same-spin doubles.  f(J, H_IJ) is called for each partner J that is
 // in the determinant list; each partner appears once.
-template <typename T, typename F>
+// FULL: the space is a full product of complete string spaces (every lookup is arithmetic).
+template <bool FULL = false, typename T, typename F>
 __device__ __forceinline__ void two_conn_visit(const Args2<T> &p, const int (&t)[4], const uint64_t (&m)[4], F &&f) {
   for (int s = 0; s < 4; s++) {
     const int sp = s >> 1, spin = s & 1, other = s ^ 1;
@@ -116,7 +121,7 @@ __device__ __forceinline__ void two_conn_visit(const Args2<T> &p, const int (&t)
       int tj[4] = {t[0], t[1], t[2], t[3]};
       tj[s] = __ldg(ls.s1_J + e);
       // single in slot s
-      const int64_t j = lookup2(p, tj);
+      const int64_t j = lookup2<T, FULL>(p, tj);
       if (j >= 0) {
         T h = __ldg(ls.s1_F + e);
         h += spin == 0 ? coul_row(p.eab[sp], np, pr, m[other]) : coul_col(p.eab[sp], np, pr, m[other]);
@@ -139,7 +144,7 @@ __device__ __forceinline__ void two_conn_visit(const Args2<T> &p, const int (&t)
         for (int64_t g = q0; g < q1; g++) {
           int tk[4] = {tj[0], tj[1], tj[2], tj[3]};
           tk[r] = __ldg(lr.s1_J + g);
-          const int64_t k = lookup2(p, tk);
+          const int64_t k = lookup2<T, FULL>(p, tk);
           if (k < 0) continue;
           const int info2 = __ldg(lr.s1_info + g);
           const int pr2 = info2 >> 1;
@@ -159,32 +164,48 @@ __device__ __forceinline__ void two_conn_visit(const Args2<T> &p, const int (&t)
     for (int64_t e = d0; e < d1; e++) {
       int tj[4] = {t[0], t[1], t[2], t[3]};
       tj[s] = __ldg(ls.s2_J + e);
-      const int64_t j = lookup2(p, tj);
+      const int64_t j = lookup2<T, FULL>(p, tj);
       if (j >= 0) f(j, __ldg(ls.s2_D + e));
     }
   }
 }
 
-template <typename T, int NV>
-__global__ void __launch_bounds__(128) sigma_two_species_kernel(Args2<T> p) {
-  const int ie = blockIdx.x;
-  const int L = p.elev[ie];
-  if (L < 0) return;
-  const int64_t nq = p.psize[L];
-  for (int64_t q = threadIdx.x; q < nq; q += blockDim.x) {
-    const int64_t I = p.ebase[ie] + q;
-    const int t[4] = {p.e_a[ie], p.e_b[ie], p.pdet_a[p.pfirst[L] + q], p.pdet_b[p.pfirst[L] + q]};
-    uint64_t m[4];
-#pragma unroll
-    for (int s = 0; s < 4; s++) m[s] = p.l[s].str[t[s]];
-    T acc[NV];
-    const T dI = (T)(p.diag[I] - p.shift);
-#pragma unroll
-    for (int v = 0; v < NV; v++) acc[v] = dI * __ldg(p.X + I * NV + v);
-    two_conn_visit(p, t, m, [&](int64_t j, T h) { axpy_gather<T, NV>(acc, h, p.X, j); });
-#pragma unroll
-    for (int v = 0; v < NV; v++) p.Y[I * NV + v] = acc[v];
+// Thread per determinant over the flat determinant list (every thread busy, whatever the block sizes).
+// FULL: string indices by division; otherwise the species-0 pair holding I is found from the pair at
+// which the CTA's first determinant lies (a few steps forward through the sorted block bases).
+template <typename T, int NV, bool FULL>
+__global__ void __launch_bounds__(128) sigma_two_species_kernel(Args2<T> p, int64_t n_dets, const int32_t *ie_first) {
+  const int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= n_dets) return;
+  int t[4];
+  if (FULL) {
+    int64_t r = I;
+    t[3] = (int)(r % p.nst[3]);
+    r /= p.nst[3];
+    t[2] = (int)(r % p.nst[2]);
+    r /= p.nst[2];
+    t[1] = (int)(r % p.nst[1]);
+    t[0] = (int)(r / p.nst[1]);
+  } else {
+    int ie = ie_first[blockIdx.x];
+    int L = p.elev[ie];
+    while (L < 0 || I >= p.ebase[ie] + p.psize[L]) L = p.elev[++ie];
+    const int64_t q = I - p.ebase[ie];
+    t[0] = p.e_a[ie];
+    t[1] = p.e_b[ie];
+    t[2] = p.pdet_a[p.pfirst[L] + q];
+    t[3] = p.pdet_b[p.pfirst[L] + q];
   }
+  uint64_t m[4];
+#pragma unroll
+  for (int s = 0; s < 4; s++) m[s] = p.l[s].str[t[s]];
+  T acc[NV];
+  const T dI = (T)(p.diag[I] - p.shift);
+#pragma unroll
+  for (int v = 0; v < NV; v++) acc[v] = dI * __ldg(p.X + I * NV + v);
+  two_conn_visit<FULL>(p, t, m, [&](int64_t j, T h) { axpy_gather<T, NV>(acc, h, p.X, j); });
+#pragma unroll
+  for (int v = 0; v < NV; v++) p.Y[I * NV + v] = acc[v];
 }
 
 // Rows of the explicit Hamiltonian (two_species_create_ham,
@@ -307,6 +328,7 @@ template <typename T> static Args2<T> make_args(pq_ci_handle *h) {
   a.pdet_a = h->d_pdet_a.as<int32_t>();
   a.pdet_b = h->d_pdet_b.as<int32_t>();
   a.diag = h->d_diag.as<double>();
+  for (int s = 0; s < 4; s++) a.nst[s] = (int)h->str[s >> 1][s & 1].size();
   return a;
 }
 
@@ -423,14 +445,31 @@ pq_status ci_build2(pq_ci_handle *h) {
       h->elev[ie] = L;
       if (L >= 0) nd += h->psize[L];
     }
-  (void)n0b;
-  (void)n1b;
+
   if (ne > INT32_MAX || nd <= 0) {
     set_error("two-species space: %lld species-0 pairs, %lld determinants", (long long)ne, (long long)nd);
     return PQ_ERR_ARG;
   }
   h->n_dets = nd;
   h->full = false;
+  // the pair holding the first determinant of every 128-determinant block of the flat list
+  {
+    std::vector<int32_t> first((size_t)((nd + 127) / 128));
+    int64_t ie = 0;
+    for (size_t b = 0; b < first.size(); b++) {
+      const int64_t I = (int64_t)b * 128;
+      while (h->elev[ie] < 0 || I >= h->ebase[ie] + h->psize[h->elev[ie]]) ie++;
+      first[b] = (int32_t)ie;
+    }
+    PQ_TRY(upload(h->d_ie_first, first, st));
+  }
+  // a full product of complete string spaces: every species-0 pair kept with the whole species-1 space
+  {
+    bool full = ne == n0a * n0b;
+    const int64_t n1 = n1a * n1b;
+    for (int64_t ie = 0; full && ie < ne; ie++) full = h->elev[ie] >= 0 && h->psize[h->elev[ie]] == n1;
+    h->full2 = full && nd == ne * n1;
+  }
   PQ_TRY(upload(h->d_rowoff, rowoff32, st));
   PQ_TRY(upload(h->d_rowlen, h->rowlen, st));
   PQ_TRY(upload(h->d_e_a, h->e_a, st));
@@ -460,8 +499,11 @@ static pq_status launch2(pq_ci_handle *h, const void *X, void *Y, double shift) 
   a.shift = shift;
   a.X = (const T *)X;
   a.Y = (T *)Y;
-  const int64_t ne = (int64_t)h->e_a.size();
-  sigma_two_species_kernel<T, NV><<<(unsigned)ne, 128, 0, h->stream>>>(a);
+  const unsigned grid = (unsigned)((h->n_dets + 127) / 128);
+  if (h->full2)
+    sigma_two_species_kernel<T, NV, true><<<grid, 128, 0, h->stream>>>(a, h->n_dets, nullptr);
+  else
+    sigma_two_species_kernel<T, NV, false><<<grid, 128, 0, h->stream>>>(a, h->n_dets, h->d_ie_first.as<int32_t>());
   PQ_CUDA_TRY(cudaGetLastError());
   return PQ_OK;
 }

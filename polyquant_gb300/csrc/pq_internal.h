@@ -119,6 +119,8 @@ struct pq_ci_handle {
   std::vector<int64_t> pfirst;          // offset of level L's (a, b) list
   std::vector<int32_t> pdet_a, pdet_b;  // species-1 (alpha, beta) of block entry q, per level
   pq::DevBuf d_e_a, d_e_b, d_ebase, d_elev, d_prowoff, d_prowlen, d_pfirst, d_psize, d_pdet_a, d_pdet_b;
+  pq::DevBuf d_ie_first;  // species-0 pair holding the first determinant of each 128-determinant block
+  bool full2 = false;     // full product of complete string spaces (arithmetic addressing)
   // integral blocks, row-major: [s] same-species alpha|beta, [se][sp] electron|positron
   pq::DevBuf d_eabs64[2], d_eabs32[2], d_ep64[2][2], d_ep32[2][2];
   // explicit Hamiltonian (ci_explicit.cu): CSR with both triangles, FP64
