@@ -266,6 +266,9 @@ def bench_ao2mo(n=256, L=1024, seed=0):
                      "rms_err": d.pow(2).mean().sqrt().item(), "max_abs_value": scale}
         del r, d
     out["fp64"] = {"ms": ms64, "tflops": flops / (ms64 * 1e-3) / 1e12}
+    from polyquant_gb300._lib import load
+
+    load().pq_ao2mo_release_workspace()  # the split modes' work buffers (about 20 GB here) are not needed after
     b = out["bf16x3"]
     cpu = cpu_ao2mo_sample(n, L, seed, synthetic.mo_coefficients(n, n, seed=seed + 1), flops)
     return {"metric": "AO->MO TFLOP/s", "value": b["tflops"], "unit": "TFLOP/s", "mode": "bf16x3",
@@ -497,6 +500,7 @@ def main():
     ap.add_argument("--no-psh", action="store_true")
     ap.add_argument("--only-ao2mo", action="store_true", help="run only the AO->MO measurement (profiling case)")
     ap.add_argument("--ao2mo-n", type=int, default=256, help="AO/MO count of the AO->MO measurement (smaller: profiling)")
+    ap.add_argument("--only-psh", action="store_true", help="run only the electron-positron measurement (profiling)")
     ap.add_argument("--tts", action="store_true", help="(default) time to 1 uEh: FP64 vs mixed Davidson")
     ap.add_argument("--no-tts", action="store_true", help="skip the time-to-solution leg")
     ap.add_argument("--batch", action="store_true", help="(default) the batched uneven-CI workload")
@@ -520,6 +524,9 @@ def main():
     torch.cuda.set_device(local)
     if args.only_ao2mo:
         print(json.dumps(bench_ao2mo(n=args.ao2mo_n)), flush=True)
+        return
+    if args.only_psh:
+        print(json.dumps({"psh_like": bench_psh_like(cpu_budget=1.0)}), flush=True)
         return
     if args.only_batch:
         print(json.dumps({"batched_ci": bench_batch(args.batch_problems)}), flush=True)

@@ -42,6 +42,14 @@ pq_status pq_ao2mo(const double *eri_ao, int32_t layout, int64_t n_ao_a, int64_t
                    int64_t ldc_a, int64_t n_mo_a, const double *C_b, int64_t ldc_b, int64_t n_mo_b, int32_t mode,
                    double *eri_mo, void *stream);
 
+/* The split-precision modes keep their work buffers (about 2.5 x the FP64
+ * pair matrix, e.g. 20 GB at n_ao = n_mo = 256) on the device between calls,
+ * so repeated transforms allocate nothing; calls on one device share them and
+ * run one at a time.  This frees them for the current device (no reference
+ * counterpart: the reference's transform holds its buffers only during the
+ * call). */
+pq_status pq_ao2mo_release_workspace(void);
+
 /* MO one-body integrals h_MO = C^T F C for an n_ao x n_ao operator F
  * (integral.cpp:166-205); DEVICE buffers, column-major. */
 pq_status pq_mo1(const double *F_ao, int64_t n_ao, const double *C, int64_t ldc, int64_t n_mo, double *h_mo,

@@ -23,6 +23,7 @@ EXPORTS = [
     "pq_ci_davidson", "pq_ci_ham_build", "pq_ci_ham_release", "pq_ci_ham_csr", "pq_ci_s2", "pq_ci_rdm1",
     "pq_ci_batch_create", "pq_ci_batch_destroy", "pq_ci_batch_num_dets", "pq_ci_batch_sigma",
     "pq_ci_batch_tuning", "pq_ci_batch_davidson", "pq_ao2mo", "pq_mo1", "pq_debug_set_wait_budget",
+    "pq_ao2mo_release_workspace",
 ]
 
 
@@ -138,6 +139,8 @@ def load(path: str = LIB_PATH):
                                        ctypes.POINTER(PQDavidsonReport)]
     L.pq_ao2mo.restype = I32
     L.pq_ao2mo.argtypes = [P, I32, I64, I64, P, I64, I64, P, I64, I64, I32, P, P]
+    L.pq_ao2mo_release_workspace.restype = I32
+    L.pq_ao2mo_release_workspace.argtypes = []
     L.pq_debug_set_wait_budget.restype = I32
     L.pq_debug_set_wait_budget.argtypes = [ctypes.c_longlong]
     L.pq_mo1.restype = I32

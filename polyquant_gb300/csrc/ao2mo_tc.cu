@@ -25,6 +25,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "pq_internal.h"
@@ -593,16 +594,34 @@ static pq_status run_gemm(const Operand &A, const Operand &B, bool a_batched, bo
   return PQ_OK;
 }
 
+// Work buffers of the split-precision transform, kept per device between calls (grow-only) so that repeated
+// transforms allocate nothing; calls on one device are serialised by the mutex (they share the buffers, and
+// each call synchronises its stream before it returns).  pq_ao2mo_release_workspace frees them.
+struct Ao2moWorkspace {
+  DevBuf full, cth, ctl, sh, sl, uh, ul, H1, H1t, Erow, err;
+};
+static std::mutex g_ws_mu;
+static Ao2moWorkspace g_ws[64];
+
 template <bool TF32>
 static pq_status ao2mo_tc_impl(const double *eri_ao, int layout, int64_t n, const double *C, int64_t ldc, int64_t nm,
                                double *eri_mo, cudaStream_t st) {
   using E = typename tc::Split<TF32>::T;
   const int64_t npa = n * (n + 1) / 2, npm = nm * (nm + 1) / 2;
   const int ld = (int)((n + 7) / 8 * 8);    // AO row length (16-byte rows for TMA)
-  DevBuf full, cth, ctl, sh, sl, uh, ul, H1, H1t, err;
+  int dev = 0;
+  PQ_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    set_error("pq_ao2mo: device ordinal %d out of range", dev);
+    return PQ_ERR_STATE;
+  }
+  std::lock_guard<std::mutex> lock(g_ws_mu);
+  Ao2moWorkspace &w = g_ws[dev];
+  DevBuf &full = w.full, &cth = w.cth, &ctl = w.ctl, &sh = w.sh, &sl = w.sl, &uh = w.uh, &ul = w.ul, &H1 = w.H1,
+         &H1t = w.H1t, &err = w.err;
   const double *pairs = eri_ao;
   if (layout == PQ_AO_PACKED8) {
-    PQ_TRY(full.alloc(sizeof(double) * npa * npa));
+    PQ_TRY(full.ensure(sizeof(double) * npa * npa));
     const unsigned nt = (unsigned)((npa + 31) / 32);
     if (nt > 65535) {
       set_error("ao2mo: too many pairs for the expansion grid");
@@ -612,21 +631,21 @@ static pq_status ao2mo_tc_impl(const double *eri_ao, int layout, int64_t n, cons
     PQ_CUDA_TRY(cudaGetLastError());
     pairs = full.as<double>();
   }
-  PQ_TRY(err.alloc(sizeof(int)));
+  PQ_TRY(err.ensure(sizeof(int)));
   PQ_CUDA_TRY(cudaMemsetAsync(err.ptr, 0, sizeof(int), st));
   // C^T split, rows = MO, row length ld (AO)
-  PQ_TRY(cth.alloc(sizeof(E) * nm * ld));
-  PQ_TRY(ctl.alloc(sizeof(E) * nm * ld));
+  PQ_TRY(cth.ensure(sizeof(E) * nm * ld));
+  PQ_TRY(ctl.ensure(sizeof(E) * nm * ld));
   tc::split_ct_kernel<TF32><<<(unsigned)((nm * ld + 255) / 256), 256, 0, st>>>(C, ldc, (int)n, (int)nm, ld, cth.as<E>(),
                                                                                ctl.as<E>());
   PQ_CUDA_TRY(cudaGetLastError());
   // slices per batch: S (n x ld) and U^T (nm x ld) in hi/lo
   const int64_t bt = std::max<int64_t>(1, std::min<int64_t>(std::max(npa, npm), 4096));
-  PQ_TRY(sh.alloc(sizeof(E) * bt * n * ld));
-  PQ_TRY(sl.alloc(sizeof(E) * bt * n * ld));
-  PQ_TRY(uh.alloc(sizeof(E) * bt * nm * ld));
-  PQ_TRY(ul.alloc(sizeof(E) * bt * nm * ld));
-  PQ_TRY(H1.alloc(sizeof(float) * npa * npm));
+  PQ_TRY(sh.ensure(sizeof(E) * bt * n * ld));
+  PQ_TRY(sl.ensure(sizeof(E) * bt * n * ld));
+  PQ_TRY(uh.ensure(sizeof(E) * bt * nm * ld));
+  PQ_TRY(ul.ensure(sizeof(E) * bt * nm * ld));
+  PQ_TRY(H1.ensure(sizeof(float) * npa * npm));
   tc::GemmArgs g{};
   g.err = err.as<int>();
   Operand ct{cth.ptr, ctl.ptr, nm, ld};
@@ -658,10 +677,10 @@ static pq_status ao2mo_tc_impl(const double *eri_ao, int layout, int64_t n, cons
   // H1t[ij][ket], in the expanded pair matrix's memory when there is one (it is not read again):
   // each reuse saves an allocation and a synchronising free inside the call
   float *h1t = nullptr;
-  if (full.ptr && full.bytes >= sizeof(float) * npa * npm) {
+  if (layout == PQ_AO_PACKED8 && full.bytes >= sizeof(float) * npa * npm) {
     h1t = full.as<float>();
   } else {
-    PQ_TRY(H1t.alloc(sizeof(float) * npa * npm));
+    PQ_TRY(H1t.ensure(sizeof(float) * npa * npm));
     h1t = H1t.as<float>();
   }
   {
@@ -674,11 +693,10 @@ static pq_status ao2mo_tc_impl(const double *eri_ao, int layout, int64_t n, cons
     PQ_CUDA_TRY(cudaGetLastError());
   }
   // half 2 over MO bra pairs: Erow[ij][kl], in H1's memory when it fits (npm <= npa); slices read from rows of H1t
-  DevBuf Erow;
   float *erow = H1.as<float>();
   if (npm > npa) {
-    PQ_TRY(Erow.alloc(sizeof(float) * npm * npm));
-    erow = Erow.as<float>();
+    PQ_TRY(w.Erow.ensure(sizeof(float) * npm * npm));
+    erow = w.Erow.as<float>();
   }
   PQ_TRY(half(nullptr, h1t, npa, npm, erow));
   {
@@ -707,6 +725,18 @@ pq_status ao2mo_tc(const double *eri_ao, int layout, int64_t n_ao, const double 
 }
 
 }  // namespace pq
+
+extern "C" pq_status pq_ao2mo_release_workspace(void) {
+  std::lock_guard<std::mutex> lock(pq::g_ws_mu);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    pq::set_error("pq_ao2mo_release_workspace: no current device");
+    return PQ_ERR_STATE;
+  }
+  pq::Ao2moWorkspace &w = pq::g_ws[dev];
+  for (pq::DevBuf *b : {&w.full, &w.cth, &w.ctl, &w.sh, &w.sl, &w.uh, &w.ul, &w.H1, &w.H1t, &w.Erow, &w.err}) b->release();
+  return PQ_OK;
+}
 
 extern "C" pq_status pq_debug_set_wait_budget(long long cycles) {
   pq::g_gemm_wait_cycles = cycles > 0 ? cycles : pq::tc::WAIT_CYCLES;

@@ -132,3 +132,28 @@ def test_gemm_wait_timeout_returns_status_and_context_survives():
         L.pq_debug_set_wait_budget(0)
     out = ao2mo(P, Cd, mode=_modes()["bf16x3"]).cpu().numpy()
     assert np.abs(out - ref).max() / np.abs(ref).max() < TOL["bf16x3"]
+
+
+def test_workspace_reused_and_released():
+    """The split-precision modes keep their work buffers between calls: a second call on the same inputs gives
+    the same numbers (no stale state), a call of another size after it is correct, and after
+    pq_ao2mo_release_workspace the next call rebuilds them."""
+    from polyquant_gb300 import _lib
+    from polyquant_gb300.integral import ao2mo
+
+    L = _lib.load()
+    out = {}
+    for n in (40, 24, 40):
+        packed, C, ref = _packed_case(n, seed=n + 1)
+        P, Cd = torch.from_numpy(packed).cuda(), torch.from_numpy(C).cuda()
+        a = ao2mo(P, Cd, mode=_modes()["bf16x3"]).cpu().numpy()
+        b = ao2mo(P, Cd, mode=_modes()["bf16x3"]).cpu().numpy()
+        assert np.array_equal(a, b)
+        assert np.abs(a - ref).max() / np.abs(ref).max() < TOL["bf16x3"]
+        out.setdefault(n, a)
+        assert np.array_equal(out[n], a)
+    assert L.pq_ao2mo_release_workspace() == _lib.PQ_OK
+    packed, C, ref = _packed_case(40, seed=41)
+    a = ao2mo(torch.from_numpy(packed).cuda(), torch.from_numpy(C).cuda(), mode=_modes()["tf32x3"]).cpu().numpy()
+    assert np.abs(a - ref).max() / np.abs(ref).max() < TOL["tf32x3"]
+    assert L.pq_ao2mo_release_workspace() == _lib.PQ_OK

@@ -86,6 +86,9 @@ def test_ao2mo_n256_rows_vs_oracle(ao2mo_n256, mode):
     out = ao2mo(packed, torch.from_numpy(C).cuda(), mode=mode_id)
     got = out[torch.from_numpy(rows).cuda()].cpu().numpy()
     del out, packed
+    from polyquant_gb300 import _lib
+
+    _lib.load().pq_ao2mo_release_workspace()
     torch.cuda.empty_cache()
     err = np.abs(got - ref).max() / np.abs(ref).max()
     assert err < AO2MO_TOL[mode], err
