@@ -92,6 +92,8 @@ pq_status ci_ham_spmv(pq_ci_handle *h, const void *X, void *Y, int nvp) {
     ham_spmv_kernel<1><<<grid, 256, 0, h->stream>>>(rp, cl, vl, n, (const double *)X, (double *)Y);
   else if (nvp == 2)
     ham_spmv_kernel<2><<<grid, 256, 0, h->stream>>>(rp, cl, vl, n, (const double *)X, (double *)Y);
+  else if (nvp == 3)
+    ham_spmv_kernel<3><<<grid, 256, 0, h->stream>>>(rp, cl, vl, n, (const double *)X, (double *)Y);
   else if (nvp == 4)
     ham_spmv_kernel<4><<<grid, 256, 0, h->stream>>>(rp, cl, vl, n, (const double *)X, (double *)Y);
   else {

@@ -47,6 +47,7 @@ template <typename T> struct Args2 {
   int npa1;       // number of species-1 alpha strings (row length of the per-level tables)
   const T *eab[2];      // [species] (pair_alpha | pair_beta) row-major
   const T *ep[2][2];    // [spin block of species 0][spin block of species 1] (pair_0 | pair_1) row-major
+  const T *epc[2][2];   // the same blocks times charge[0] * charge[1] (the cross doubles' coefficient)
   int blk[2][2];        // [species][spin] -> spin block index
   T cf;                 // charge[0] * charge[1]
   const int32_t *rowoff0, *rowlen0;
@@ -100,6 +101,12 @@ template <typename T> __device__ __forceinline__ T coul_col(const T *M, int ld, 
   return s;
 }
 
+// v or -v selected by the low bit of `neg`, on the integer pipe (a negation would be an FP64 instruction)
+__device__ __forceinline__ float flip2(float v, uint32_t neg) { return __int_as_float(__float_as_int(v) ^ (int)(neg << 31)); }
+__device__ __forceinline__ double flip2(double v, uint32_t neg) {
+  return __hiloint2double(__double2hiint(v) ^ (int)(neg << 31), __double2loint(v));
+}
+
 // Every off-diagonal connection of determinant t (string indices per slot,
 // strings m) in the classes of the reference's singleshot builder: singles of
 // each of the four spin lists with their same-species and cross-species
@@ -134,7 +141,7 @@ __device__ __forceinline__ void two_conn_visit(const Args2<T> &p, const int (&t)
           x += coul_col(p.ep[p.blk[0][1]][p.blk[1][spin]], p.npair[1], pr, m[1]);
         }
         h += p.cf * x;
-        if (neg) h = -h;
+        h = flip2(h, neg);
         f(j, h);
       }
       // single x single in a later slot r
@@ -152,9 +159,9 @@ __device__ __forceinline__ void two_conn_visit(const Args2<T> &p, const int (&t)
           if ((r >> 1) == sp) {  // alpha-beta double within one species
             c = __ldg(p.eab[sp] + (int64_t)pr * np + pr2);
           } else {                // cross-species double: species-0 slot s, species-1 slot r
-            c = p.cf * __ldg(p.ep[p.blk[0][spin]][p.blk[1][r & 1]] + (int64_t)pr * p.npair[1] + pr2);
+            c = __ldg(p.epc[p.blk[0][spin]][p.blk[1][r & 1]] + (int64_t)pr * p.npair[1] + pr2);
           }
-          if (neg ^ (uint32_t)(info2 & 1)) c = -c;
+          c = flip2(c, neg ^ (uint32_t)(info2 & 1));
           f(k, c);
         }
       }
@@ -312,7 +319,10 @@ template <typename T> static Args2<T> make_args(pq_ci_handle *h) {
     for (int spin = 0; spin < 2; spin++) a.blk[sp][spin] = spin % h->n_blocks[sp];
   }
   for (int x = 0; x < 2; x++)
-    for (int y = 0; y < 2; y++) a.ep[x][y] = (const T *)(dbl ? h->d_ep64[x][y].ptr : h->d_ep32[x][y].ptr);
+    for (int y = 0; y < 2; y++) {
+      a.ep[x][y] = (const T *)(dbl ? h->d_ep64[x][y].ptr : h->d_ep32[x][y].ptr);
+      a.epc[x][y] = (const T *)(dbl ? h->d_epc64[x][y].ptr : h->d_epc32[x][y].ptr);
+    }
   a.npa1 = (int)h->str[1][0].size();
   a.cf = (T)(h->desc.charge[0] * h->desc.charge[1]);
   a.rowoff0 = h->d_rowoff.as<int32_t>();
@@ -332,13 +342,17 @@ template <typename T> static Args2<T> make_args(pq_ci_handle *h) {
   return a;
 }
 
-static pq_status upload_rm(DevBuf &b64, DevBuf &b32, const double *colmajor, int rows, int cols, cudaStream_t st) {
+// row-major FP64 and FP32 copies of a column-major block, times `scale`; the uploads are synchronised here
+// because the host vectors are released on return
+static pq_status upload_rm(DevBuf &b64, DevBuf &b32, const double *colmajor, int rows, int cols, cudaStream_t st,
+                           double scale = 1.0) {
   std::vector<double> rm((size_t)rows * cols);
   for (int r = 0; r < rows; r++)
-    for (int c = 0; c < cols; c++) rm[(size_t)r * cols + c] = colmajor[(size_t)r + (size_t)c * rows];
+    for (int c = 0; c < cols; c++) rm[(size_t)r * cols + c] = scale * colmajor[(size_t)r + (size_t)c * rows];
   PQ_TRY(upload(b64, rm, st));
   std::vector<float> f(rm.begin(), rm.end());
   PQ_TRY(upload(b32, f, st));
+  PQ_CUDA_TRY(cudaStreamSynchronize(st));
   return PQ_OK;
 }
 
@@ -385,6 +399,8 @@ pq_status ci_build2(pq_ci_handle *h) {
         return PQ_ERR_ARG;
       }
       PQ_TRY(upload_rm(h->d_ep64[x][y], h->d_ep32[x][y], ep, h->npair[0], h->npair[1], st));
+      PQ_TRY(upload_rm(h->d_epc64[x][y], h->d_epc32[x][y], ep, h->npair[0], h->npair[1], st,
+                       d.charge[0] * d.charge[1]));
     }
   // addressing
   const std::vector<int32_t> &l0a = h->lvl[0][0], &l0b = h->lvl[0][1], &l1a = h->lvl[1][0], &l1b = h->lvl[1][1];
@@ -512,10 +528,12 @@ pq_status ci_sigma2_il(pq_ci_handle *h, const void *X, void *Y, int nvp, int pre
   if (precision == PQ_FP64) {
     if (nvp == 1) return launch2<double, 1>(h, X, Y, shift);
     if (nvp == 2) return launch2<double, 2>(h, X, Y, shift);
+    if (nvp == 3) return launch2<double, 3>(h, X, Y, shift);
     if (nvp == 4) return launch2<double, 4>(h, X, Y, shift);
   } else if (precision == PQ_FP32) {
     if (nvp == 1) return launch2<float, 1>(h, X, Y, shift);
     if (nvp == 2) return launch2<float, 2>(h, X, Y, shift);
+    if (nvp == 3) return launch2<float, 3>(h, X, Y, shift);
     if (nvp == 4) return launch2<float, 4>(h, X, Y, shift);
   }
   set_error("unsupported interleave width %d / precision %d", nvp, precision);

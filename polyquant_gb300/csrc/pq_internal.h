@@ -123,6 +123,7 @@ struct pq_ci_handle {
   bool full2 = false;     // full product of complete string spaces (arithmetic addressing)
   // integral blocks, row-major: [s] same-species alpha|beta, [se][sp] electron|positron
   pq::DevBuf d_eabs64[2], d_eabs32[2], d_ep64[2][2], d_ep32[2][2];
+  pq::DevBuf d_epc64[2][2], d_epc32[2][2];  // cross blocks times charge[0] * charge[1]
   // explicit Hamiltonian (ci_explicit.cu): CSR with both triangles, FP64
   pq::DevBuf d_hrow, d_hcol, d_hval;
   int64_t h_nnz = 0;
@@ -154,6 +155,12 @@ pq_status ci_ham_spmv(pq_ci_handle *h, const void *X, void *Y, int nvp);
 pq_status ci_unit_columns(pq_ci_handle *h, const std::vector<int64_t> &dets, double *W);
 // ci_element.cu: exact H_IJ of n pairs (host index arrays, host output)
 pq_status ci_elements(pq_ci_handle *h, int64_t n, const int64_t *I, const int64_t *J, double *out);
+// interleave width of a block of nv <= 4 vectors: 1, 2 or 4; two-species spaces also take 3 (their sigma
+// gathers root by root, so a padded fourth root would only add work)
+inline int il_width(const pq_ci_handle *h, int nv) {
+  if (nv == 3 && h->n_species == 2) return 3;
+  return nv == 1 ? 1 : (nv == 2 ? 2 : 4);
+}
 // ci_sigma32.cu
 bool sigma32_v2_applicable(const pq_ci_handle *h);
 pq_status ci_sigma32_v2(pq_ci_handle *h, const void *X, void *Y, int nvp, double shift);

@@ -60,7 +60,7 @@ def test_diagonal(case):
     assert np.abs(d - d_ref).max() <= 1e-12 * np.abs(d_ref).max()
 
 
-@pytest.mark.parametrize("nvec", [1, 2, 4])
+@pytest.mark.parametrize("nvec", [1, 2, 3, 4, 7])
 def test_sigma_fp64(case, nvec):
     _, p, ref, g = case
     C = np.random.default_rng(nvec).standard_normal((ref.n_dets, nvec))
