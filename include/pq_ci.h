@@ -48,7 +48,8 @@ const char *pq_version(void);
 
 /*
  * One CI problem, in the reference's conventions.
- *  n_orb        active orbitals per species (POLYQUANT_DETSET::max_orb)
+ *  n_orb        active orbitals per species (POLYQUANT_DETSET::max_orb), 1..128;
+ *               strings of more than 64 orbitals are held as two words
  *  n_alpha/beta active particles per spin (frozen core already removed)
  *  restricted   1: one spin block of integrals (the reference's `1 % size` rule)
  *  charge       species charge; cross-species terms carry charge[0]*charge[1]

@@ -88,10 +88,12 @@ pq_status pq_ci_strings(const pq_ci_handle *h, int32_t species, int32_t spin, ui
   if (n_words) *n_words = h->n_words;
   if (words) {
     // reference layout: orbital o lives in word n_words-1-(o>>6), bit o&63
+    const std::vector<uint64_t> &hi = h->str_hi[species][spin];
     int nw = h->n_words;
     for (size_t i = 0; i < s.size(); i++) {
       for (int w = 0; w < nw; w++) words[i * nw + w] = 0;
       words[i * nw + (nw - 1)] = s[i];
+      if (h->wide) words[i * nw + (nw - 2)] = hi[i];
     }
   }
   return PQ_OK;

@@ -818,6 +818,10 @@ pq_status make_prob(pq_ci_handle *h, BatchTables &bt, Prob &pr, cudaStream_t st)
     set_error("pq_ci_batch: %d species-1 determinants exceed the batched kernel's limit of %d", P, MAX_P);
     return PQ_ERR_ARG;
   }
+  if (h->wide) {
+    set_error("pq_ci_batch: batched problems hold at most 64 orbitals per species (one-word strings)");
+    return PQ_ERR_ARG;
+  }
   pr = Prob{};
   const SpinTablesDev &A = h->tab[0][0], &B = h->tab[0][1];
   pr.astr = A.str.as<uint64_t>();

@@ -5,12 +5,14 @@
 // through the excitation tables of ci_setup.cu).  Shared by the exact
 // unit-vector columns and the explicit sparse Hamiltonian.
 #pragma once
+#include "pq_bits.cuh"
 #include "pq_internal.h"
 
 namespace pq {
 
 struct ConnArgs {
   const uint64_t *astr, *bstr;
+  const uint64_t *astr_hi, *bstr_hi;  // orbitals 64..127 (NULL for one-word strings)
   const int64_t *a1_off, *a2_off, *b1_off, *b2_off;
   const int32_t *a1_J, *a1_info, *a2_J, *b1_J, *b1_info, *b2_J;
   const double *a1_F, *a2_D, *b1_F, *b2_D;
@@ -26,6 +28,8 @@ inline ConnArgs make_conn_args(const pq_ci_handle *h) {
   const SpinTablesDev &A = h->tab[0][0], &B = h->tab[0][1];
   a.astr = A.str.as<uint64_t>();
   a.bstr = B.str.as<uint64_t>();
+  a.astr_hi = A.str_hi.as<uint64_t>();
+  a.bstr_hi = B.str_hi.as<uint64_t>();
   a.a1_off = A.s1_off.as<int64_t>();
   a.a2_off = A.s2_off.as<int64_t>();
   a.b1_off = B.s1_off.as<int64_t>();
@@ -53,7 +57,7 @@ struct ConnRow {
   int ia, ib;
   int64_t I, a1b, a2b, b1b, b2b;
   int n1a, n2a, n1b, n2b;
-  uint64_t am, bm;
+  uint64_t am, bm, amh, bmh;  // occupation words (lo, hi) of the alpha and beta strings
   __device__ __forceinline__ int64_t total() const { return 1 + (int64_t)n1a + n1b + n2a + n2b + (int64_t)n1a * n1b; }
 };
 
@@ -72,6 +76,8 @@ __device__ __forceinline__ ConnRow conn_row(const ConnArgs &a, int ia, int ib) {
   r.n2b = (int)(a.b2_off[ib + 1] - r.b2b);
   r.am = a.astr[ia];
   r.bm = a.bstr[ib];
+  r.amh = hiword(a.astr_hi, ia);
+  r.bmh = hiword(a.bstr_hi, ib);
   return r;
 }
 
@@ -87,19 +93,13 @@ __device__ __forceinline__ int64_t conn_elem(const ConnArgs &a, const ConnRow &r
   } else if ((t -= 1) < r.n1a) {
     const int Ja = a.a1_J[r.a1b + t], info = a.a1_info[r.a1b + t], ph = info >> 1;
     double f = a.a1_F[r.a1b + t];
-    for (uint64_t m = r.bm; m; m &= m - 1) {
-      const int k = __ffsll((long long)m) - 1;
-      f += a.eab[(int64_t)ph * a.npair + k * (k + 3) / 2];
-    }
+    for_occ(r.bm, r.bmh, [&](int k) { f += a.eab[(int64_t)ph * a.npair + k * (k + 3) / 2]; });
     x = (info & 1) ? -f : f;
     if (r.ib < a.rowlen[Ja]) J = a.rowoff[Ja] + r.ib;
   } else if ((t -= r.n1a) < r.n1b) {
     const int Jb = a.b1_J[r.b1b + t], info = a.b1_info[r.b1b + t], ph = info >> 1;
     double f = a.b1_F[r.b1b + t];
-    for (uint64_t m = r.am; m; m &= m - 1) {
-      const int k = __ffsll((long long)m) - 1;
-      f += a.eab[(int64_t)(k * (k + 3) / 2) * a.npair + ph];
-    }
+    for_occ(r.am, r.amh, [&](int k) { f += a.eab[(int64_t)(k * (k + 3) / 2) * a.npair + ph]; });
     x = (info & 1) ? -f : f;
     if (Jb < a.rowlen[r.ia]) J = a.rowoff[r.ia] + Jb;
   } else if ((t -= r.n1b) < r.n2a) {

@@ -19,6 +19,7 @@
 #include <algorithm>
 
 #include "ci_conn.cuh"
+#include "pq_bits.cuh"
 #include "pq_internal.h"
 
 namespace pq {
@@ -38,21 +39,23 @@ __global__ void __launch_bounds__(PROP_THREADS) s2_kernel(ConnArgs a, int na, co
     double cI[S2_MAXV];
 #pragma unroll
     for (int v = 0; v < S2_MAXV; v++) cI[v] = v < nvec ? C[r.I + v * ldc] : 0.0;
-    const uint64_t open = r.am ^ r.bm;
-    const int n_open = __popcll(open), n_a = __popcll(open & r.am);
+    const uint64_t open = r.am ^ r.bm, openh = r.amh ^ r.bmh;
+    const int n_open = popc2(open, openh), n_a = popc2(open & r.am, openh & r.amh);
     const double sz = n_a - 0.5 * n_open;
     const double d = n_a + sz * (sz - 1.0);
 #pragma unroll
     for (int v = 0; v < S2_MAXV; v++) acc[v] += cI[v] * cI[v] * d;
     for (int s = 0; s < r.n1a; s++) {
       const int Ja = a.a1_J[r.a1b + s], infa = a.a1_info[r.a1b + s];
-      const uint64_t jam = a.astr[Ja];
-      const int ha = __ffsll((long long)(r.am & ~jam)) - 1, pa = __ffsll((long long)(jam & ~r.am)) - 1;
-      if (!((r.bm >> pa) & 1ULL) || ((r.bm >> ha) & 1ULL)) continue;
-      const uint64_t jbm = r.bm ^ (1ULL << pa) ^ (1ULL << ha);
+      const uint64_t jam = a.astr[Ja], jamh = hiword(a.astr_hi, Ja);
+      const int ha = first_set(r.am & ~jam, r.amh & ~jamh), pa = first_set(jam & ~r.am, jamh & ~r.amh);
+      if (!occupied(r.bm, r.bmh, pa) || occupied(r.bm, r.bmh, ha)) continue;
+      uint64_t jbm = r.bm, jbmh = r.bmh;
+      flip_orb(jbm, jbmh, pa);
+      flip_orb(jbm, jbmh, ha);
       for (int q = 0; q < r.n1b; q++) {
         const int Jb = a.b1_J[r.b1b + q];
-        if (a.bstr[Jb] != jbm) continue;
+        if (a.bstr[Jb] != jbm || hiword(a.bstr_hi, Jb) != jbmh) continue;
         if (Jb < a.rowlen[Ja]) {
           const int64_t J = a.rowoff[Ja] + Jb;
           const double ph = ((infa ^ a.b1_info[r.b1b + q]) & 1) ? -1.0 : 1.0;
@@ -89,33 +92,31 @@ __global__ void __launch_bounds__(PROP_THREADS) rdm1_kernel(ConnArgs a, int na, 
   for (int ib = blockIdx.y * blockDim.x + threadIdx.x; ia < na && ib < a.rowlen[ia]; ib += gridDim.y * blockDim.x) {
     const ConnRow r = conn_row(a, ia, ib);
     const double cI = C[r.I];
-    const uint64_t mine = spin == 0 ? r.am : r.bm;
+    const uint64_t mine = spin == 0 ? r.am : r.bm, mineh = spin == 0 ? r.amh : r.bmh;
     const double c2 = cI * cI;
-    if (fabs(c2) > 1e-16)
-      for (uint64_t m = mine; m; m &= m - 1) {
-        const int o = __ffsll((long long)m) - 1;
-        atomicAdd(acc + o * (n + 1), c2);
-      }
+    if (fabs(c2) > 1e-16) for_occ(mine, mineh, [&](int o) { atomicAdd(acc + o * (n + 1), c2); });
     const int ns = spin == 0 ? r.n1a : r.n1b;
     for (int s = 0; s < ns; s++) {
       int64_t J = -1;
       int info;
-      uint64_t jm;
+      uint64_t jm, jmh;
       if (spin == 0) {
         const int Ja = a.a1_J[r.a1b + s];
         info = a.a1_info[r.a1b + s];
         jm = a.astr[Ja];
+        jmh = hiword(a.astr_hi, Ja);
         if (r.ib < a.rowlen[Ja]) J = a.rowoff[Ja] + r.ib;
       } else {
         const int Jb = a.b1_J[r.b1b + s];
         info = a.b1_info[r.b1b + s];
         jm = a.bstr[Jb];
+        jmh = hiword(a.bstr_hi, Jb);
         if (Jb < a.rowlen[r.ia]) J = a.rowoff[r.ia] + Jb;
       }
       if (J < 0 || J > r.I) continue;  // each pair once, from the later determinant
       const double c = ((info & 1) ? -cI : cI) * C[J];
       if (fabs(c) <= 1e-16) continue;
-      const int k = __ffsll((long long)(mine & ~jm)) - 1, l = __ffsll((long long)(jm & ~mine)) - 1;
+      const int k = first_set(mine & ~jm, mineh & ~jmh), l = first_set(jm & ~mine, jmh & ~mineh);
       atomicAdd(acc + k + l * n, c);
       atomicAdd(acc + l + k * n, c);
     }
@@ -131,7 +132,7 @@ struct TwoAddr {
   const int32_t *e_a, *e_b, *elev, *rowoff0, *rowlen0, *prowoff, *prowlen, *pdet_a, *pdet_b;
   const int64_t *ebase, *pfirst, *psize;
   int npa1;
-  const uint64_t *str[2][2];
+  const uint64_t *str[2][2], *str_hi[2][2];  // str_hi: orbitals 64..127 (NULL for one-word strings)
   const int64_t *s1_off[2][2];
   const int32_t *s1_J[2][2], *s1_info[2][2];
 };
@@ -161,11 +162,12 @@ __global__ void __launch_bounds__(PROP_THREADS) s2_two_kernel(TwoAddr t, int sp,
     const int64_t I = t.ebase[ie] + q;
     const int ia = d[2 * sp], ib = d[2 * sp + 1];
     const uint64_t am = t.str[sp][0][ia], bm = t.str[sp][1][ib];
+    const uint64_t amh = hiword(t.str_hi[sp][0], ia), bmh = hiword(t.str_hi[sp][1], ib);
     double cI[S2_MAXV];
 #pragma unroll
     for (int v = 0; v < S2_MAXV; v++) cI[v] = v < nvec ? C[I + v * ldc] : 0.0;
-    const uint64_t open = am ^ bm;
-    const int n_open = __popcll(open), n_a = __popcll(open & am);
+    const uint64_t open = am ^ bm, openh = amh ^ bmh;
+    const int n_open = popc2(open, openh), n_a = popc2(open & am, openh & amh);
     const double sz = n_a - 0.5 * n_open;
     const double dg = n_a + sz * (sz - 1.0);
 #pragma unroll
@@ -174,13 +176,15 @@ __global__ void __launch_bounds__(PROP_THREADS) s2_two_kernel(TwoAddr t, int sp,
     const int n1a = (int)(t.s1_off[sp][0][ia + 1] - a1b), n1b = (int)(t.s1_off[sp][1][ib + 1] - b1b);
     for (int s = 0; s < n1a; s++) {
       const int Ja = t.s1_J[sp][0][a1b + s], infa = t.s1_info[sp][0][a1b + s];
-      const uint64_t jam = t.str[sp][0][Ja];
-      const int ha = __ffsll((long long)(am & ~jam)) - 1, pa = __ffsll((long long)(jam & ~am)) - 1;
-      if (!((bm >> pa) & 1ULL) || ((bm >> ha) & 1ULL)) continue;
-      const uint64_t jbm = bm ^ (1ULL << pa) ^ (1ULL << ha);
+      const uint64_t jam = t.str[sp][0][Ja], jamh = hiword(t.str_hi[sp][0], Ja);
+      const int ha = first_set(am & ~jam, amh & ~jamh), pa = first_set(jam & ~am, jamh & ~amh);
+      if (!occupied(bm, bmh, pa) || occupied(bm, bmh, ha)) continue;
+      uint64_t jbm = bm, jbmh = bmh;
+      flip_orb(jbm, jbmh, pa);
+      flip_orb(jbm, jbmh, ha);
       for (int q2 = 0; q2 < n1b; q2++) {
         const int Jb = t.s1_J[sp][1][b1b + q2];
-        if (t.str[sp][1][Jb] != jbm) continue;
+        if (t.str[sp][1][Jb] != jbm || hiword(t.str_hi[sp][1], Jb) != jbmh) continue;
         int e[4] = {d[0], d[1], d[2], d[3]};
         e[2 * sp] = Ja;
         e[2 * sp + 1] = Jb;
@@ -223,10 +227,9 @@ __global__ void __launch_bounds__(PROP_THREADS) rdm1_two_kernel(TwoAddr t, int s
     const int64_t I = t.ebase[ie] + q;
     const double cI = C[I];
     const int si = d[2 * sp + spin];
-    const uint64_t mine = t.str[sp][spin][si];
+    const uint64_t mine = t.str[sp][spin][si], mineh = hiword(t.str_hi[sp][spin], si);
     const double c2 = cI * cI;
-    if (fabs(c2) > 1e-16)
-      for (uint64_t m = mine; m; m &= m - 1) atomicAdd(acc + (__ffsll((long long)m) - 1) * (n + 1), c2);
+    if (fabs(c2) > 1e-16) for_occ(mine, mineh, [&](int o) { atomicAdd(acc + o * (n + 1), c2); });
     const int64_t b = t.s1_off[sp][spin][si];
     const int ns = (int)(t.s1_off[sp][spin][si + 1] - b);
     for (int s = 0; s < ns; s++) {
@@ -237,8 +240,8 @@ __global__ void __launch_bounds__(PROP_THREADS) rdm1_two_kernel(TwoAddr t, int s
       if (J < 0 || J > I) continue;  // each pair once, from the later determinant
       const double c = ((info & 1) ? -cI : cI) * C[J];
       if (fabs(c) <= 1e-16) continue;
-      const uint64_t jm = t.str[sp][spin][Js];
-      const int k = __ffsll((long long)(mine & ~jm)) - 1, l = __ffsll((long long)(jm & ~mine)) - 1;
+      const uint64_t jm = t.str[sp][spin][Js], jmh = hiword(t.str_hi[sp][spin], Js);
+      const int k = first_set(mine & ~jm, mineh & ~jmh), l = first_set(jm & ~mine, jmh & ~mineh);
       atomicAdd(acc + k + l * n, c);
       atomicAdd(acc + l + k * n, c);
     }
@@ -266,6 +269,7 @@ static TwoAddr make_two(const pq_ci_handle *h) {
   for (int s = 0; s < 2; s++)
     for (int sp = 0; sp < 2; sp++) {
       t.str[s][sp] = h->tab[s][sp].str.as<uint64_t>();
+      t.str_hi[s][sp] = h->tab[s][sp].str_hi.as<uint64_t>();
       t.s1_off[s][sp] = h->tab[s][sp].s1_off.as<int64_t>();
       t.s1_J[s][sp] = h->tab[s][sp].s1_J.as<int32_t>();
       t.s1_info[s][sp] = h->tab[s][sp].s1_info.as<int32_t>();

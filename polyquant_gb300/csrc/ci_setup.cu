@@ -17,6 +17,7 @@
 #include <cstring>
 #include <numeric>
 
+#include "pq_bits.cuh"
 #include "pq_internal.h"
 
 namespace pq {
@@ -36,15 +37,18 @@ pq_status DevBuf::alloc(size_t n) {
 
 __host__ __device__ inline int idx2(int i, int j) { return i > j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i; }
 
-// Occupied orbitals of d strictly between lo and hi (lo < hi <= 63).
-__host__ __device__ inline int between_count(uint64_t d, int lo, int hi) {
+// bits 0 .. k-1 of a 64-bit word (k in 0..64)
+__host__ __device__ inline uint64_t low_bits(int k) { return k <= 0 ? 0ULL : (k >= 64 ? ~0ULL : ((1ULL << k) - 1ULL)); }
+
+// Occupied orbitals of the string (dl: orbitals 0..63, dh: 64..127) strictly between lo and hi (lo < hi).
+__host__ __device__ inline int between_count(uint64_t dl, uint64_t dh, int lo, int hi) {
   if (hi - lo <= 1) return 0;
-  uint64_t below_hi = (hi >= 64) ? ~0ULL : ((1ULL << hi) - 1ULL);
-  uint64_t upto_lo = (lo + 1 >= 64) ? ~0ULL : ((1ULL << (lo + 1)) - 1ULL);
+  const uint64_t ml = low_bits(hi) & ~low_bits(lo + 1);
+  const uint64_t mh = low_bits(hi - 64) & ~low_bits(lo + 1 - 64);
 #ifdef __CUDA_ARCH__
-  return __popcll(d & below_hi & ~upto_lo);
+  return __popcll(dl & ml) + __popcll(dh & mh);
 #else
-  return __builtin_popcountll(d & below_hi & ~upto_lo);
+  return __builtin_popcountll(dl & ml) + __builtin_popcountll(dh & mh);
 #endif
 }
 
@@ -62,13 +66,24 @@ static bool next_comb(std::vector<int> &c, int n) {
   return true;
 }
 
-pq_status make_strings(int n_orb, int n_e, int ex_max, std::vector<uint64_t> &out, std::vector<int32_t> &lvl) {
+pq_status make_strings(int n_orb, int n_e, int ex_max, std::vector<uint64_t> &out, std::vector<int32_t> &lvl,
+                       std::vector<uint64_t> *out_hi) {
   out.clear();
   lvl.clear();
-  uint64_t hf = 0;
-  for (int i = 0; i < n_e; i++) hf |= 1ULL << i;
-  out.push_back(hf);
-  lvl.push_back(0);
+  if (out_hi) out_hi->clear();
+  if (n_orb > 64 && !out_hi) {
+    set_error("make_strings: %d orbitals need two words", n_orb);
+    return PQ_ERR_ARG;
+  }
+  typedef unsigned __int128 u128;
+  auto push = [&](u128 t, int k) {
+    out.push_back((uint64_t)t);
+    if (out_hi) out_hi->push_back((uint64_t)(t >> 64));
+    lvl.push_back(k);
+  };
+  u128 hf = 0;
+  for (int i = 0; i < n_e; i++) hf |= (u128)1 << i;
+  push(hf, 0);
   int n_virt = n_orb - n_e;
   for (int k = 1; k <= ex_max; k++) {
     if (k > n_virt) {
@@ -81,11 +96,10 @@ pq_status make_strings(int n_orb, int n_e, int ex_max, std::vector<uint64_t> &ou
     do {
       std::iota(cv.begin(), cv.end(), 0);
       do {
-        uint64_t t = hf;
-        for (int i = 0; i < k; i++) t &= ~(1ULL << co[i]);
-        for (int i = 0; i < k; i++) t |= 1ULL << (n_e + cv[i]);
-        out.push_back(t);
-        lvl.push_back(k);
+        u128 t = hf;
+        for (int i = 0; i < k; i++) t &= ~((u128)1 << co[i]);
+        for (int i = 0; i < k; i++) t |= (u128)1 << (n_e + cv[i]);
+        push(t, k);
       } while (next_comb(cv, n_virt));
     } while (next_comb(co, n_e));
     if (out.size() > (size_t)INT32_MAX) {
@@ -98,22 +112,25 @@ pq_status make_strings(int n_orb, int n_e, int ex_max, std::vector<uint64_t> &ou
 
 // ---------------------------------------------------------------------------
 // device: replacement tables.  One thread per string.
-__device__ inline int64_t find_string(const uint64_t *sorted, const int32_t *perm, int64_t n, uint64_t key) {
+// index of the string (kl, kh) among strings sorted by (hi word, lo word); -1 when absent
+__device__ inline int64_t find_string(const uint64_t *sorted, const uint64_t *sorted_hi, const int32_t *perm, int64_t n,
+                                      uint64_t kl, uint64_t kh) {
   int64_t lo = 0, hi = n;
   while (lo < hi) {
     int64_t mid = (lo + hi) >> 1;
-    if (sorted[mid] < key)
+    const uint64_t mh = hiword(sorted_hi, mid);
+    if (mh < kh || (mh == kh && sorted[mid] < kl))
       lo = mid + 1;
     else
       hi = mid;
   }
-  return (lo < n && sorted[lo] == key) ? perm[lo] : -1;
+  return (lo < n && sorted[lo] == kl && hiword(sorted_hi, lo) == kh) ? perm[lo] : -1;
 }
 
 struct TableArgs {
   int64_t n_str;
-  const uint64_t *masks;
-  const uint64_t *sorted;
+  const uint64_t *masks, *masks_hi;
+  const uint64_t *sorted, *sorted_hi;
   const int32_t *perm;
   int n_orb, npair;
   const double *h1;   // n x n column-major
@@ -131,18 +148,23 @@ template <bool COUNT>
 __global__ void __launch_bounds__(128) spin_tables_kernel(TableArgs a) {
   int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= a.n_str) return;
-  const uint64_t m = a.masks[I];
+  const uint64_t m = a.masks[I], mh = hiword(a.masks_hi, I);
   const int n = a.n_orb;
-  const uint64_t all = (n >= 64) ? ~0ULL : ((1ULL << n) - 1ULL);
-  int occ[64], vir[64];
+  int occ[128], vir[128];
   int no = 0, nv = 0;
   for (int o = 0; o < n; o++) {
-    if ((m >> o) & 1ULL)
+    if (occupied(m, mh, o))
       occ[no++] = o;
     else
       vir[nv++] = o;
   }
-  (void)all;
+  // flip orbital o of the string (jl, jh)
+  auto flip = [](uint64_t &jl, uint64_t &jh, int o) {
+    if (o < 64)
+      jl ^= 1ULL << o;
+    else
+      jh ^= 1ULL << (o - 64);
+  };
   auto E = [&](int r, int c) { return a.eri[(int64_t)r + (int64_t)c * a.npair]; };
   int32_t c1 = 0, c2 = 0;
   int64_t w1 = COUNT ? 0 : a.off1[I], w2 = COUNT ? 0 : a.off2[I];
@@ -151,15 +173,17 @@ __global__ void __launch_bounds__(128) spin_tables_kernel(TableArgs a) {
     int hh = occ[x];
     for (int y = 0; y < nv; y++) {
       int pp = vir[y];
-      uint64_t jm = m ^ (1ULL << hh) ^ (1ULL << pp);
-      int64_t J = find_string(a.sorted, a.perm, a.n_str, jm);
+      uint64_t jm = m, jh = mh;
+      flip(jm, jh, hh);
+      flip(jm, jh, pp);
+      int64_t J = find_string(a.sorted, a.sorted_hi, a.perm, a.n_str, jm, jh);
       if (J < 0) continue;
       if (COUNT) {
         c1++;
         continue;
       }
       int lo = hh < pp ? hh : pp, hi = hh < pp ? pp : hh;
-      int neg = between_count(m, lo, hi) & 1;
+      int neg = between_count(m, mh, lo, hi) & 1;
       int php = idx2(hh, pp);
       double f = a.h1[hh + (int64_t)pp * n];
       for (int z = 0; z < no; z++) {
@@ -179,8 +203,12 @@ __global__ void __launch_bounds__(128) spin_tables_kernel(TableArgs a) {
       for (int y0 = 0; y0 < nv; y0++)
         for (int y1 = y0 + 1; y1 < nv; y1++) {
           int p0 = vir[y0], p1 = vir[y1];
-          uint64_t jm = m ^ (1ULL << h0) ^ (1ULL << h1) ^ (1ULL << p0) ^ (1ULL << p1);
-          int64_t J = find_string(a.sorted, a.perm, a.n_str, jm);
+          uint64_t jm = m, jh = mh;
+          flip(jm, jh, h0);
+          flip(jm, jh, h1);
+          flip(jm, jh, p0);
+          flip(jm, jh, p1);
+          int64_t J = find_string(a.sorted, a.sorted_hi, a.perm, a.n_str, jm, jh);
           if (J < 0) continue;
           if (COUNT) {
             c2++;
@@ -189,7 +217,7 @@ __global__ void __launch_bounds__(128) spin_tables_kernel(TableArgs a) {
           // phase: pairs (h0,p0), (h1,p1) after sorting holes and particles
           int a0 = h0 < p0 ? h0 : p0, b0 = h0 < p0 ? p0 : h0;
           int a1 = h1 < p1 ? h1 : p1, b1 = h1 < p1 ? p1 : h1;
-          int nperm = between_count(m, a0, b0) + between_count(m, a1, b1);
+          int nperm = between_count(m, mh, a0, b0) + between_count(m, mh, a1, b1);
           if (a0 < a1 && a1 < b0 && b0 < b1) nperm++;
           double v = E(idx2(h0, p0), idx2(h1, p1)) - E(idx2(h0, p1), idx2(h1, p0));
           a.J2[w2] = (int32_t)J;
@@ -224,28 +252,22 @@ __global__ void to_float_kernel(const double *src, float *dst, int64_t n) {
 // string, chunk of beta strings); the alpha row of the Coulomb sum is staged in
 // shared memory.
 __global__ void __launch_bounds__(256) diag_kernel(int64_t nblk_b, const int64_t *rowoff, const int32_t *rowlen,
-                                                   const uint64_t *ma, const uint64_t *mb, const double *ea,
-                                                   const double *eb, const double *eab, int npair, int n_orb,
-                                                   double *diag) {
-  __shared__ double u[64];
+                                                   const uint64_t *ma, const uint64_t *ma_hi, const uint64_t *mb,
+                                                   const uint64_t *mb_hi, const double *ea, const double *eb,
+                                                   const double *eab, int npair, int n_orb, double *diag) {
+  __shared__ double u[128];
   int64_t Ia = blockIdx.x / nblk_b;
   int64_t Ib = (blockIdx.x % nblk_b) * blockDim.x + threadIdx.x;
-  uint64_t a = ma[Ia];
+  const uint64_t al = ma[Ia], ah = hiword(ma_hi, Ia);
   for (int j = threadIdx.x; j < n_orb; j += blockDim.x) {
     double s = 0.0;
-    for (int i = 0; i < n_orb; i++)
-      if ((a >> i) & 1ULL) s += eab[(int64_t)idx2(i, i) * npair + idx2(j, j)];
+    for_occ(al, ah, [&](int i) { s += eab[(int64_t)idx2(i, i) * npair + idx2(j, j)]; });
     u[j] = s;
   }
   __syncthreads();
   if (Ib >= rowlen[Ia]) return;
-  uint64_t b = mb[Ib];
   double e = ea[Ia] + eb[Ib];
-  while (b) {
-    int j = __ffsll((long long)b) - 1;
-    e += u[j];
-    b &= b - 1;
-  }
+  for_occ(mb[Ib], hiword(mb_hi, Ib), [&](int j) { e += u[j]; });
   diag[rowoff[Ia] + Ib] = e;
 }
 
@@ -254,16 +276,28 @@ pq_status build_spin_tables(pq_ci_handle *h, int s, int sp, const double *h1_hos
   cudaStream_t st = h->stream;
   SpinTablesDev &T = h->tab[s][sp];
   const std::vector<uint64_t> &masks = h->str[s][sp];
+  const std::vector<uint64_t> &mhi = h->str_hi[s][sp];
+  const bool two = h->wide;
   int64_t n = (int64_t)masks.size();
   T.n_str = n;
   int no = h->n_orb[s], npair = h->npair[s];
   std::vector<int32_t> perm(n);
   std::iota(perm.begin(), perm.end(), 0);
-  std::sort(perm.begin(), perm.end(), [&](int32_t x, int32_t y) { return masks[x] < masks[y]; });
-  std::vector<uint64_t> sorted(n);
-  for (int64_t i = 0; i < n; i++) sorted[i] = masks[perm[i]];
-  DevBuf d_sorted, d_perm, d_h1, d_eri, d_cnt1, d_cnt2;
+  auto hw = [&](int64_t i) { return two ? mhi[i] : 0ULL; };
+  std::sort(perm.begin(), perm.end(), [&](int32_t x, int32_t y) {
+    return hw(x) < hw(y) || (hw(x) == hw(y) && masks[x] < masks[y]);
+  });
+  std::vector<uint64_t> sorted(n), sorted_hi(two ? n : 0);
+  for (int64_t i = 0; i < n; i++) {
+    sorted[i] = masks[perm[i]];
+    if (two) sorted_hi[i] = mhi[perm[i]];
+  }
+  DevBuf d_sorted, d_sorted_hi, d_perm, d_h1, d_eri, d_cnt1, d_cnt2;
   PQ_TRY(upload(T.str, masks, st));
+  if (two) {
+    PQ_TRY(upload(T.str_hi, mhi, st));
+    PQ_TRY(upload(d_sorted_hi, sorted_hi, st));
+  }
   PQ_TRY(upload(d_sorted, sorted, st));
   PQ_TRY(upload(d_perm, perm, st));
   PQ_TRY(d_h1.alloc(sizeof(double) * no * no));
@@ -276,7 +310,9 @@ pq_status build_spin_tables(pq_ci_handle *h, int s, int sp, const double *h1_hos
   TableArgs a{};
   a.n_str = n;
   a.masks = T.str.as<uint64_t>();
+  a.masks_hi = two ? T.str_hi.as<uint64_t>() : nullptr;
   a.sorted = d_sorted.as<uint64_t>();
+  a.sorted_hi = two ? d_sorted_hi.as<uint64_t>() : nullptr;
   a.perm = d_perm.as<int32_t>();
   a.n_orb = no;
   a.npair = npair;
@@ -338,8 +374,8 @@ pq_status ci_build(pq_ci_handle *h) {
   }
   int maxorb = 0;
   for (int s = 0; s < d.n_species; s++) {
-    if (d.n_orb[s] < 1 || d.n_orb[s] > 64) {
-      set_error("n_orb[%d]=%d outside 1..64", s, d.n_orb[s]);
+    if (d.n_orb[s] < 1 || d.n_orb[s] > PQ_MAX_ORB) {
+      set_error("n_orb[%d]=%d outside 1..%d", s, d.n_orb[s], PQ_MAX_ORB);
       return PQ_ERR_ARG;
     }
     if (d.n_alpha[s] < 0 || d.n_beta[s] < 0 || d.n_alpha[s] > d.n_orb[s] || d.n_beta[s] > d.n_orb[s]) {
@@ -350,12 +386,17 @@ pq_status ci_build(pq_ci_handle *h) {
     h->npair[s] = d.n_orb[s] * (d.n_orb[s] + 1) / 2;
     h->n_blocks[s] = d.restricted[s] ? 1 : 2;
     maxorb = std::max(maxorb, d.n_orb[s]);
-    int ne[2] = {d.n_alpha[s], d.n_beta[s]};
-    for (int sp = 0; sp < 2; sp++) {
-      PQ_TRY(make_strings(d.n_orb[s], ne[sp], d.ex_level[s][sp], h->str[s][sp], h->lvl[s][sp]));
-    }
   }
+  // the reference's word count: n_words = (max_orb >> 6) + 1 (determinant_creation.cpp:13); internally a
+  // second word is kept only when some species has more than 64 orbitals
   h->n_words = (maxorb >> 6) + 1;
+  h->wide = maxorb > 64;
+  for (int s = 0; s < d.n_species; s++) {
+    int ne[2] = {d.n_alpha[s], d.n_beta[s]};
+    for (int sp = 0; sp < 2; sp++)
+      PQ_TRY(make_strings(d.n_orb[s], ne[sp], d.ex_level[s][sp], h->str[s][sp], h->lvl[s][sp],
+                          h->wide ? &h->str_hi[s][sp] : nullptr));
+  }
   // integral blocks: alpha index 0, beta index 1 % n_blocks (slater_condon_singleparticle.cpp:11)
   const int A = 0, B = 1 % h->n_blocks[0];
   const double *h1a = d.h1[0][A], *h1b = d.h1[0][B];
@@ -404,7 +445,8 @@ pq_status ci_build(pq_ci_handle *h) {
   int64_t nblk_b = (nb + 255) / 256;
   if (h->n_dets > 0) {
     diag_kernel<<<(unsigned)(na * nblk_b), 256, 0, st>>>(nblk_b, h->d_rowoff.as<int64_t>(), h->d_rowlen.as<int32_t>(),
-                                                         h->tab[0][0].str.as<uint64_t>(), h->tab[0][1].str.as<uint64_t>(),
+                                                         h->tab[0][0].str.as<uint64_t>(), h->tab[0][0].str_hi.as<uint64_t>(),
+                                                         h->tab[0][1].str.as<uint64_t>(), h->tab[0][1].str_hi.as<uint64_t>(),
                                                          h->tab[0][0].e_same64.as<double>(),
                                                          h->tab[0][1].e_same64.as<double>(), h->d_eab64.as<double>(),
                                                          npair, h->n_orb[0], h->d_diag.as<double>());

@@ -13,13 +13,15 @@
 // thread <-> determinant (Ia, Ib).  Everything that depends only on Ia is
 // staged once per CTA in shared memory:
 //   Wa[pair]        = sum_{k in occ(Ia)} (kk|pair)_ab  (opposite-spin Coulomb of beta singles)
-//   Jrow[e][k]      = (pair_e|kk)_ab for the CTA's alpha singles e
+//   Jrow[e][k]      = (pair_e|kk)_ab for the CTA's alpha singles e (read from
+//                     the integrals in global memory when it does not fit)
 //   Tab[e][pair_b]  = sign_e (pair_e|pair_b)_ab        (alpha-beta doubles)
 // C/sigma are interleaved by determinant (X[det*NV + v]) so one vector load
 // fetches all roots of a determinant.
 #include <algorithm>
 
 #include "ci_conn.cuh"
+#include "pq_bits.cuh"
 #include "pq_internal.h"
 
 namespace pq {
@@ -27,7 +29,7 @@ namespace pq {
 __device__ __forceinline__ int idx2d(int i, int j) { return i > j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i; }
 
 template <typename T> struct SpinView {
-  const uint64_t *str;
+  const uint64_t *str, *str_hi;  // str_hi: orbitals 64..127 (NULL for one-word strings)
   const int64_t *s1_off;
   const int32_t *s1_J;
   const int32_t *s1_info;
@@ -45,6 +47,7 @@ template <typename T> struct SigmaArgs {
   const double *diag;
   double shift;
   int n_orb, npair, max1a;
+  int jrow_global;  // the alpha singles' Coulomb rows are read from eab instead of shared memory
   int64_t nblk_b;
   const T *X;
   T *Y;
@@ -124,26 +127,21 @@ __global__ void __launch_bounds__(SIGMA_THREADS, (PK > 0 ? 2 : 1)) sigma_one_spe
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *Wa = reinterpret_cast<T *>(smem_raw);
   T *Jrow = Wa + p.npair;
-  T *Tab = Jrow + p.max1a * p.n_orb;
+  T *Tab = Jrow + (p.jrow_global ? 0 : p.max1a * p.n_orb);
 
   const int64_t Ia = blockIdx.x / p.nblk_b;
   const int Ib = (int)(blockIdx.x % p.nblk_b) * SIGMA_THREADS + threadIdx.x;
-  const uint64_t ma = p.a.str[Ia];
+  const uint64_t ma = p.a.str[Ia], mah = hiword(p.a.str_hi, Ia);
   const int64_t a1_0 = p.a.s1_off[Ia];
   const int na1 = (int)(p.a.s1_off[Ia + 1] - a1_0);
   const int npair = p.npair, n_orb = p.n_orb;
 
   for (int q = threadIdx.x; q < npair; q += SIGMA_THREADS) {
     T s = 0;
-    uint64_t m = ma;
-    while (m) {
-      int k = __ffsll((long long)m) - 1;
-      s += p.eab[(int64_t)idx2d(k, k) * npair + q];
-      m &= m - 1;
-    }
+    for_occ(ma, mah, [&](int k) { s += p.eab[(int64_t)idx2d(k, k) * npair + q]; });
     Wa[q] = s;
   }
-  for (int t = threadIdx.x; t < na1 * n_orb; t += SIGMA_THREADS) {
+  for (int t = threadIdx.x; t < (p.jrow_global ? 0 : na1 * n_orb); t += SIGMA_THREADS) {
     int e = t / n_orb, k = t - e * n_orb;
     int pa = p.a.s1_info[a1_0 + e] >> 1;
     Jrow[t] = p.eab[(int64_t)pa * npair + idx2d(k, k)];
@@ -162,7 +160,7 @@ __global__ void __launch_bounds__(SIGMA_THREADS, (PK > 0 ? 2 : 1)) sigma_one_spe
   if (Ib >= lenI) return;
   const int64_t rowI = p.rowoff[Ia];
   const int64_t I = rowI + Ib;
-  const uint64_t mb = p.b.str[Ib];
+  const uint64_t mb = p.b.str[Ib], mbh = hiword(p.b.str_hi, Ib);
 
   T acc[NV];
   {
@@ -197,12 +195,12 @@ __global__ void __launch_bounds__(SIGMA_THREADS, (PK > 0 ? 2 : 1)) sigma_one_spe
     if (!FULL && Ib >= __ldg(p.rowlen + Ja)) continue;
     const int info = __ldg(p.a.s1_info + a1_0 + e);
     T hv = __ldg(p.a.s1_F + a1_0 + e);
-    uint64_t m = mb;
-    const T *jr = Jrow + e * n_orb;
-    while (m) {
-      int k = __ffsll((long long)m) - 1;
-      hv += jr[k];
-      m &= m - 1;
+    if (p.jrow_global) {
+      const T *er = p.eab + (int64_t)(info >> 1) * npair;
+      for_occ(mb, mbh, [&](int k) { hv += __ldg(er + idx2d(k, k)); });
+    } else {
+      const T *jr = Jrow + e * n_orb;
+      for_occ(mb, mbh, [&](int k) { hv += jr[k]; });
     }
     if (info & 1) hv = -hv;
     fma_vec<T, NV>(acc, hv, p.X + (__ldg(p.rowoff + Ja) + Ib) * NV);
@@ -285,12 +283,12 @@ __global__ void __launch_bounds__(SIGMA_THREADS, (PK > 0 ? 2 : 1)) sigma_one_spe
 template <typename T>
 static SpinView<T> make_view(const SpinTablesDev &t);
 template <> SpinView<double> make_view<double>(const SpinTablesDev &t) {
-  return {t.str.as<uint64_t>(), t.s1_off.as<int64_t>(), t.s1_J.as<int32_t>(), t.s1_info.as<int32_t>(),
-          t.s1_F64.as<double>(), t.s2_off.as<int64_t>(), t.s2_J.as<int32_t>(), t.s2_D64.as<double>()};
+  return {t.str.as<uint64_t>(), t.str_hi.as<uint64_t>(), t.s1_off.as<int64_t>(), t.s1_J.as<int32_t>(),
+          t.s1_info.as<int32_t>(), t.s1_F64.as<double>(), t.s2_off.as<int64_t>(), t.s2_J.as<int32_t>(), t.s2_D64.as<double>()};
 }
 template <> SpinView<float> make_view<float>(const SpinTablesDev &t) {
-  return {t.str.as<uint64_t>(), t.s1_off.as<int64_t>(), t.s1_J.as<int32_t>(), t.s1_info.as<int32_t>(),
-          t.s1_F32.as<float>(), t.s2_off.as<int64_t>(), t.s2_J.as<int32_t>(), t.s2_D32.as<float>()};
+  return {t.str.as<uint64_t>(), t.str_hi.as<uint64_t>(), t.s1_off.as<int64_t>(), t.s1_J.as<int32_t>(),
+          t.s1_info.as<int32_t>(), t.s1_F32.as<float>(), t.s2_off.as<int64_t>(), t.s2_J.as<int32_t>(), t.s2_D32.as<float>()};
 }
 
 template <typename T, int NV, bool FULL, bool TAB, int PK>
@@ -327,6 +325,9 @@ static pq_status sigma_dispatch(pq_ci_handle *h, const T *X, T *Y, double shift)
   size_t base = sizeof(T) * ((size_t)a.npair + (size_t)a.max1a * a.n_orb);
   size_t tab = sizeof(T) * (size_t)a.max1a * a.npair;
   const bool use_tab = base + tab <= 100 * 1024;
+  // large orbital spaces: the Coulomb rows of the alpha singles stay in global memory (L2)
+  a.jrow_global = base > 160 * 1024;
+  if (a.jrow_global) base = sizeof(T) * (size_t)a.npair;
   size_t smem = base + (use_tab ? tab : 0);
   if (smem > 200 * 1024) {
     set_error("sigma shared-memory staging %zu bytes too large", smem);

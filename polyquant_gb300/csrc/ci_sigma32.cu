@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(128) ab_scatter_kernel(ABArgs p) {
 
 // ---------------------------------------------------------------------------
 bool sigma32_v2_applicable(const pq_ci_handle *h) {
-  if (h->n_species != 1 || !h->full) return false;
+  if (h->n_species != 1 || !h->full || h->wide) return false;
   const int npair = h->npair[0];
   if (h->tab[0][0].max1 > AB_MAXI || h->tab[0][1].max1 > AB_MAXI) return false;
   const size_t wbytes = sizeof(float) * (size_t)AB_MAXI * npair;

@@ -24,6 +24,7 @@
 // alpha-beta doubles within a species, single x single cross doubles).
 #include <algorithm>
 
+#include "pq_bits.cuh"
 #include "pq_internal.h"
 
 namespace pq {
@@ -31,7 +32,7 @@ namespace pq {
 __device__ __forceinline__ int tri2(int i, int j) { return i > j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i; }
 
 template <typename T> struct List2 {
-  const uint64_t *str;
+  const uint64_t *str, *str_hi;  // str_hi: orbitals 64..127 (NULL for one-word strings)
   const int64_t *s1_off;
   const int32_t *s1_J;
   const int32_t *s1_info;
@@ -81,24 +82,27 @@ template <typename T, int NV> __device__ __forceinline__ void axpy_gather(T (&ac
   for (int v = 0; v < NV; v++) acc[v] = fma(c, __ldg(X + j * NV + v), acc[v]);
 }
 
-// sum over occupied orbitals k of `m` of M[row * ld + tri(k,k)] (row fixed) or M[tri(k,k) * ld + col]
-template <typename T> __device__ __forceinline__ T coul_row(const T *M, int ld, int row, uint64_t m) {
+// sum over occupied orbitals k of the string (m, mh) of M[row * ld + tri(k,k)] (row fixed) or
+// M[tri(k,k) * ld + col]
+template <typename T> __device__ __forceinline__ T coul_row(const T *M, int ld, int row, uint64_t m, uint64_t mh) {
   T s = 0;
-  while (m) {
-    int k = __ffsll((long long)m) - 1;
-    s += __ldg(M + (int64_t)row * ld + tri2(k, k));
-    m &= m - 1;
-  }
+  for_occ(m, mh, [&](int k) { s += __ldg(M + (int64_t)row * ld + tri2(k, k)); });
   return s;
 }
-template <typename T> __device__ __forceinline__ T coul_col(const T *M, int ld, int col, uint64_t m) {
+template <typename T> __device__ __forceinline__ T coul_col(const T *M, int ld, int col, uint64_t m, uint64_t mh) {
   T s = 0;
-  while (m) {
-    int k = __ffsll((long long)m) - 1;
-    s += __ldg(M + (int64_t)tri2(k, k) * ld + col);
-    m &= m - 1;
-  }
+  for_occ(m, mh, [&](int k) { s += __ldg(M + (int64_t)tri2(k, k) * ld + col); });
   return s;
+}
+
+// occupation words (lo, hi) of the four strings of determinant t
+template <typename T>
+__device__ __forceinline__ void load_words(const Args2<T> &p, const int (&t)[4], uint64_t (&m)[4], uint64_t (&mh)[4]) {
+#pragma unroll
+  for (int s = 0; s < 4; s++) {
+    m[s] = p.l[s].str[t[s]];
+    mh[s] = hiword(p.l[s].str_hi, t[s]);
+  }
 }
 
 // v or -v selected by the low bit of `neg`, on the integer pipe (a negation would be an FP64 instruction)
@@ -108,14 +112,15 @@ __device__ __forceinline__ double flip2(double v, uint32_t neg) {
 }
 
 // Every off-diagonal connection of determinant t (string indices per slot,
-// strings m) in the classes of the reference's singleshot builder: singles of
+// occupation words m, mh) in the classes of the reference's singleshot builder: singles of
 // each of the four spin lists with their same-species and cross-species
 // Coulomb terms, alpha-beta doubles within a species, single x single cross
 // doubles, same-spin doubles.  f(J, H_IJ) is called for each partner J that is
 // in the determinant list; each partner appears once.
 // FULL: the space is a full product of complete string spaces (every lookup is arithmetic).
 template <bool FULL = false, typename T, typename F>
-__device__ __forceinline__ void two_conn_visit(const Args2<T> &p, const int (&t)[4], const uint64_t (&m)[4], F &&f) {
+__device__ __forceinline__ void two_conn_visit(const Args2<T> &p, const int (&t)[4], const uint64_t (&m)[4],
+                                               const uint64_t (&mh)[4], F &&f) {
   for (int s = 0; s < 4; s++) {
     const int sp = s >> 1, spin = s & 1, other = s ^ 1;
     const List2<T> &ls = p.l[s];
@@ -131,14 +136,15 @@ __device__ __forceinline__ void two_conn_visit(const Args2<T> &p, const int (&t)
       const int64_t j = lookup2<T, FULL>(p, tj);
       if (j >= 0) {
         T h = __ldg(ls.s1_F + e);
-        h += spin == 0 ? coul_row(p.eab[sp], np, pr, m[other]) : coul_col(p.eab[sp], np, pr, m[other]);
+        h += spin == 0 ? coul_row(p.eab[sp], np, pr, m[other], mh[other])
+                       : coul_col(p.eab[sp], np, pr, m[other], mh[other]);
         T x = 0;
         if (sp == 0) {
-          x += coul_row(p.ep[p.blk[0][spin]][p.blk[1][0]], p.npair[1], pr, m[2]);
-          x += coul_row(p.ep[p.blk[0][spin]][p.blk[1][1]], p.npair[1], pr, m[3]);
+          x += coul_row(p.ep[p.blk[0][spin]][p.blk[1][0]], p.npair[1], pr, m[2], mh[2]);
+          x += coul_row(p.ep[p.blk[0][spin]][p.blk[1][1]], p.npair[1], pr, m[3], mh[3]);
         } else {
-          x += coul_col(p.ep[p.blk[0][0]][p.blk[1][spin]], p.npair[1], pr, m[0]);
-          x += coul_col(p.ep[p.blk[0][1]][p.blk[1][spin]], p.npair[1], pr, m[1]);
+          x += coul_col(p.ep[p.blk[0][0]][p.blk[1][spin]], p.npair[1], pr, m[0], mh[0]);
+          x += coul_col(p.ep[p.blk[0][1]][p.blk[1][spin]], p.npair[1], pr, m[1], mh[1]);
         }
         h += p.cf * x;
         h = flip2(h, neg);
@@ -180,7 +186,8 @@ __device__ __forceinline__ void two_conn_visit(const Args2<T> &p, const int (&t)
 // Thread per determinant over the flat determinant list (every thread busy, whatever the block sizes).
 // FULL: string indices by division; otherwise the species-0 pair holding I is found from the pair at
 // which the CTA's first determinant lies (a few steps forward through the sorted block bases).
-template <typename T, int NV, bool FULL>
+// WIDE: strings of more than 64 orbitals (two words); one-word spaces keep the hi words at compile-time zero.
+template <typename T, int NV, bool FULL, bool WIDE>
 __global__ void __launch_bounds__(128) sigma_two_species_kernel(Args2<T> p, int64_t n_dets, const int32_t *ie_first) {
   const int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= n_dets) return;
@@ -203,14 +210,21 @@ __global__ void __launch_bounds__(128) sigma_two_species_kernel(Args2<T> p, int6
     t[2] = p.pdet_a[p.pfirst[L] + q];
     t[3] = p.pdet_b[p.pfirst[L] + q];
   }
-  uint64_t m[4];
+  uint64_t m[4], mh[4];
+  if (WIDE) {
+    load_words(p, t, m, mh);
+  } else {
 #pragma unroll
-  for (int s = 0; s < 4; s++) m[s] = p.l[s].str[t[s]];
+    for (int s = 0; s < 4; s++) {
+      m[s] = p.l[s].str[t[s]];
+      mh[s] = 0;
+    }
+  }
   T acc[NV];
   const T dI = (T)(p.diag[I] - p.shift);
 #pragma unroll
   for (int v = 0; v < NV; v++) acc[v] = dI * __ldg(p.X + I * NV + v);
-  two_conn_visit<FULL>(p, t, m, [&](int64_t j, T h) { axpy_gather<T, NV>(acc, h, p.X, j); });
+  two_conn_visit<FULL>(p, t, m, mh, [&](int64_t j, T h) { axpy_gather<T, NV>(acc, h, p.X, j); });
 #pragma unroll
   for (int v = 0; v < NV; v++) p.Y[I * NV + v] = acc[v];
 }
@@ -230,9 +244,8 @@ __global__ void __launch_bounds__(128) ham_rows_two_kernel(Args2<double> p, doub
   for (int64_t q = threadIdx.x; q < nq; q += blockDim.x) {
     const int64_t I = p.ebase[ie] + q;
     const int t[4] = {p.e_a[ie], p.e_b[ie], p.pdet_a[p.pfirst[L] + q], p.pdet_b[p.pfirst[L] + q]};
-    uint64_t m[4];
-#pragma unroll
-    for (int s = 0; s < 4; s++) m[s] = p.l[s].str[t[s]];
+    uint64_t m[4], mh[4];
+    load_words(p, t, m, mh);
     int64_t w = FILL ? row_ptr[I] : 0;
     int32_t c = 0;
     auto emit = [&](int64_t j, double h) {
@@ -247,7 +260,7 @@ __global__ void __launch_bounds__(128) ham_rows_two_kernel(Args2<double> p, doub
       }
     };
     emit(I, p.diag[I]);
-    two_conn_visit(p, t, m, emit);
+    two_conn_visit(p, t, m, mh, emit);
     if (!FILL) cnt[I] = c;
   }
 }
@@ -263,30 +276,20 @@ __global__ void __launch_bounds__(128) diag_two_kernel(Args2<double> p, const do
   const double *es[4] = {es0, es1, es2, es3};
   for (int64_t q = threadIdx.x; q < nq; q += blockDim.x) {
     const int t[4] = {p.e_a[ie], p.e_b[ie], p.pdet_a[p.pfirst[L] + q], p.pdet_b[p.pfirst[L] + q]};
-    uint64_t m[4];
+    uint64_t m[4], mh[4];
+    load_words(p, t, m, mh);
     double e = 0.0;
-    for (int s = 0; s < 4; s++) {
-      m[s] = p.l[s].str[t[s]];
-      e += es[s][t[s]];
-    }
-    for (int sp = 0; sp < 2; sp++) {
-      uint64_t a = m[2 * sp];
-      while (a) {
-        int i = __ffsll((long long)a) - 1;
-        e += coul_row(p.eab[sp], p.npair[sp], tri2(i, i), m[2 * sp + 1]);
-        a &= a - 1;
-      }
-    }
+    for (int s = 0; s < 4; s++) e += es[s][t[s]];
+    for (int sp = 0; sp < 2; sp++)
+      for_occ(m[2 * sp], mh[2 * sp], [&](int i) {
+        e += coul_row(p.eab[sp], p.npair[sp], tri2(i, i), m[2 * sp + 1], mh[2 * sp + 1]);
+      });
     double x = 0.0;
     for (int se = 0; se < 2; se++)
-      for (int spn = 0; spn < 2; spn++) {
-        uint64_t a = m[se];
-        while (a) {
-          int i = __ffsll((long long)a) - 1;
-          x += coul_row(p.ep[p.blk[0][se]][p.blk[1][spn]], p.npair[1], tri2(i, i), m[2 + spn]);
-          a &= a - 1;
-        }
-      }
+      for (int spn = 0; spn < 2; spn++)
+        for_occ(m[se], mh[se], [&](int i) {
+          x += coul_row(p.ep[p.blk[0][se]][p.blk[1][spn]], p.npair[1], tri2(i, i), m[2 + spn], mh[2 + spn]);
+        });
     diag[p.ebase[ie] + q] = e + p.cf * x;
   }
 }
@@ -295,12 +298,12 @@ __global__ void __launch_bounds__(128) diag_two_kernel(Args2<double> p, const do
 template <typename T> static Args2<T> make_args(pq_ci_handle *h);
 
 static List2<double> view64(const SpinTablesDev &t) {
-  return {t.str.as<uint64_t>(), t.s1_off.as<int64_t>(), t.s1_J.as<int32_t>(), t.s1_info.as<int32_t>(),
-          t.s1_F64.as<double>(), t.s2_off.as<int64_t>(), t.s2_J.as<int32_t>(), t.s2_D64.as<double>()};
+  return {t.str.as<uint64_t>(), t.str_hi.as<uint64_t>(), t.s1_off.as<int64_t>(), t.s1_J.as<int32_t>(),
+          t.s1_info.as<int32_t>(), t.s1_F64.as<double>(), t.s2_off.as<int64_t>(), t.s2_J.as<int32_t>(), t.s2_D64.as<double>()};
 }
 static List2<float> view32(const SpinTablesDev &t) {
-  return {t.str.as<uint64_t>(), t.s1_off.as<int64_t>(), t.s1_J.as<int32_t>(), t.s1_info.as<int32_t>(),
-          t.s1_F32.as<float>(), t.s2_off.as<int64_t>(), t.s2_J.as<int32_t>(), t.s2_D32.as<float>()};
+  return {t.str.as<uint64_t>(), t.str_hi.as<uint64_t>(), t.s1_off.as<int64_t>(), t.s1_J.as<int32_t>(),
+          t.s1_info.as<int32_t>(), t.s1_F32.as<float>(), t.s2_off.as<int64_t>(), t.s2_J.as<int32_t>(), t.s2_D32.as<float>()};
 }
 
 template <typename T> static Args2<T> make_args(pq_ci_handle *h) {
@@ -361,8 +364,8 @@ pq_status ci_build2(pq_ci_handle *h) {
   cudaStream_t st = h->stream;
   int maxorb = 0;
   for (int s = 0; s < 2; s++) {
-    if (d.n_orb[s] < 1 || d.n_orb[s] > 64) {
-      set_error("n_orb[%d]=%d outside 1..64", s, d.n_orb[s]);
+    if (d.n_orb[s] < 1 || d.n_orb[s] > PQ_MAX_ORB) {
+      set_error("n_orb[%d]=%d outside 1..%d", s, d.n_orb[s], PQ_MAX_ORB);
       return PQ_ERR_ARG;
     }
     if (d.n_alpha[s] < 0 || d.n_beta[s] < 0 || d.n_alpha[s] > d.n_orb[s] || d.n_beta[s] > d.n_orb[s]) {
@@ -373,10 +376,15 @@ pq_status ci_build2(pq_ci_handle *h) {
     h->npair[s] = d.n_orb[s] * (d.n_orb[s] + 1) / 2;
     h->n_blocks[s] = d.restricted[s] ? 1 : 2;
     maxorb = std::max(maxorb, d.n_orb[s]);
-    int ne[2] = {d.n_alpha[s], d.n_beta[s]};
-    for (int sp = 0; sp < 2; sp++) PQ_TRY(make_strings(d.n_orb[s], ne[sp], d.ex_level[s][sp], h->str[s][sp], h->lvl[s][sp]));
   }
   h->n_words = (maxorb >> 6) + 1;
+  h->wide = maxorb > 64;
+  for (int s = 0; s < 2; s++) {
+    int ne[2] = {d.n_alpha[s], d.n_beta[s]};
+    for (int sp = 0; sp < 2; sp++)
+      PQ_TRY(make_strings(d.n_orb[s], ne[sp], d.ex_level[s][sp], h->str[s][sp], h->lvl[s][sp],
+                          h->wide ? &h->str_hi[s][sp] : nullptr));
+  }
   // integral blocks
   for (int s = 0; s < 2; s++) {
     const int A = 0, B = 1 % h->n_blocks[s];
@@ -516,10 +524,13 @@ static pq_status launch2(pq_ci_handle *h, const void *X, void *Y, double shift) 
   a.X = (const T *)X;
   a.Y = (T *)Y;
   const unsigned grid = (unsigned)((h->n_dets + 127) / 128);
-  if (h->full2)
-    sigma_two_species_kernel<T, NV, true><<<grid, 128, 0, h->stream>>>(a, h->n_dets, nullptr);
+  // wide strings take the searched addressing, which holds for full products too
+  if (h->wide)
+    sigma_two_species_kernel<T, NV, false, true><<<grid, 128, 0, h->stream>>>(a, h->n_dets, h->d_ie_first.as<int32_t>());
+  else if (h->full2)
+    sigma_two_species_kernel<T, NV, true, false><<<grid, 128, 0, h->stream>>>(a, h->n_dets, nullptr);
   else
-    sigma_two_species_kernel<T, NV, false><<<grid, 128, 0, h->stream>>>(a, h->n_dets, h->d_ie_first.as<int32_t>());
+    sigma_two_species_kernel<T, NV, false, false><<<grid, 128, 0, h->stream>>>(a, h->n_dets, h->d_ie_first.as<int32_t>());
   PQ_CUDA_TRY(cudaGetLastError());
   return PQ_OK;
 }
@@ -564,10 +575,9 @@ __global__ void elements_two_kernel(Args2<double> p, int64_t n, const int32_t *t
     v = p.diag[target];
   } else {
     const int t[4] = {t4[4 * i], t4[4 * i + 1], t4[4 * i + 2], t4[4 * i + 3]};
-    uint64_t m[4];
-#pragma unroll
-    for (int s = 0; s < 4; s++) m[s] = p.l[s].str[t[s]];
-    two_conn_visit(p, t, m, [&](int64_t j, double h) {
+    uint64_t m[4], mh[4];
+    load_words(p, t, m, mh);
+    two_conn_visit(p, t, m, mh, [&](int64_t j, double h) {
       if (j == target) v = h;
     });
   }

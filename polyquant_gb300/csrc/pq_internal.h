@@ -12,6 +12,9 @@
 
 struct cublasContext;  // cuBLAS handle type (cublasHandle_t)
 
+// Orbitals per species: strings are held as at most two 64-bit words.
+#define PQ_MAX_ORB 128
+
 namespace pq {
 
 // Thread-local error message behind pq_last_error().
@@ -66,7 +69,8 @@ struct SpinTablesDev {
   int64_t n_str = 0;
   int64_t n1 = 0, n2 = 0;  // total entries
   int32_t max1 = 0, max2 = 0;
-  DevBuf str;              // uint64 occupation masks, bit o = orbital o
+  DevBuf str;              // uint64 occupation masks, bit o = orbital o (orbitals 0..63)
+  DevBuf str_hi;           // orbitals 64..127, bit o - 64 (allocated only for wide strings)
   DevBuf s1_off, s1_J, s1_info, s1_F64, s1_F32;
   DevBuf s2_off, s2_J, s2_D64, s2_D32;
   DevBuf e_same64;         // per-string same-spin energy (diagonal part)
@@ -80,10 +84,12 @@ struct pq_ci_handle {
   int n_species = 1;
   int n_orb[2] = {0, 0};
   int npair[2] = {0, 0};
-  int n_words = 1;
+  int n_words = 1;     // words per string in the reference layout, (max n_orb >> 6) + 1
+  bool wide = false;   // some species has more than 64 orbitals: strings keep a second word
   int n_blocks[2] = {1, 1};  // spin blocks of integrals per species
   // host strings (occupation masks, reference order) and their levels
   std::vector<uint64_t> str[2][2];
+  std::vector<uint64_t> str_hi[2][2];  // orbitals 64..127 of each string (wide only)
   std::vector<int32_t> lvl[2][2];
   // determinant addressing over species-0 alpha strings (single species)
   int64_t n_dets = 0;
@@ -133,7 +139,8 @@ struct pq_ci_handle {
 namespace pq {
 // ci_setup.cu
 pq_status ci_build(pq_ci_handle *h);
-pq_status make_strings(int n_orb, int n_e, int ex_max, std::vector<uint64_t> &out, std::vector<int32_t> &lvl);
+pq_status make_strings(int n_orb, int n_e, int ex_max, std::vector<uint64_t> &out, std::vector<int32_t> &lvl,
+                       std::vector<uint64_t> *out_hi = nullptr);
 pq_status build_spin_tables(pq_ci_handle *h, int s, int sp, const double *h1_host, const double *eri_host);
 // ci_two.cu (electron + positron product space)
 pq_status ci_build2(pq_ci_handle *h);
