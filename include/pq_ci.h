@@ -102,10 +102,12 @@ pq_status pq_ci_diag(pq_ci_handle *h, double *out_device);
  * arithmetic, inputs/outputs still FP64). */
 pq_status pq_ci_sigma(pq_ci_handle *h, const double *C, int64_t ldc, int32_t nvec, double *S, int64_t lds,
                       int32_t precision);
-/* Same with HOST buffers: copies in, computes, copies out (blocking).  The
- * device copies of C and sigma are kept by the handle and reused by later
- * calls (released with the handle); page-locked host buffers give full copy
- * bandwidth. */
+/* Same with HOST buffers (blocking).  Page-locked buffers (cudaHostAlloc or
+ * cudaHostRegister) are read and written in place by the layout-conversion
+ * kernels, so C streams straight from host memory into the interleaved work
+ * vectors and sigma straight back.  Pageable buffers are staged: the device
+ * copies of C and sigma are kept by the handle and reused by later calls
+ * (released with the handle). */
 pq_status pq_ci_sigma_host(pq_ci_handle *h, const double *C, int64_t ldc, int32_t nvec, double *S, int64_t lds,
                            int32_t precision);
 

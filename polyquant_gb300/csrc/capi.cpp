@@ -3,6 +3,7 @@
 // live here; the work is in the .cu translation units.
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -158,6 +159,16 @@ pq_status pq_ci_sigma(pq_ci_handle *h, const double *C, int64_t ldc, int32_t nve
   return sigma_device(h, C, ldc, nvec, S, lds, precision);
 }
 
+// Device address of a page-locked (pinned or registered) host buffer; NULL for pageable memory.
+static const void *mapped_host(const void *p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // clear the sticky-free error of an unknown pointer
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 pq_status pq_ci_sigma_host(pq_ci_handle *h, const double *C, int64_t ldc, int32_t nvec, double *S, int64_t lds,
                            int32_t precision) {
   clear_error();
@@ -167,8 +178,17 @@ pq_status pq_ci_sigma_host(pq_ci_handle *h, const double *C, int64_t ldc, int32_
     return PQ_ERR_ARG;
   }
   int64_t n = h->n_dets;
-  // device copies of C and sigma stay with the handle (grow-only), so repeated calls allocate nothing;
-  // with ldc == n (and lds == n) each block moves in one copy
+  // Page-locked buffers are read and written in place: the layout conversions around sigma load C from host
+  // memory and store sigma back to it (over NVLink-C2C on Grace), so nothing is staged and the transfers run
+  // on all SMs instead of one copy engine.
+  const void *mc = mapped_host(C), *ms = mapped_host(S);
+  if (mc && ms && getenv("PQ_SIGMA_HOST_STAGED") == nullptr) {
+    PQ_TRY(sigma_device(h, (const double *)mc, ldc, nvec, (double *)ms, lds, precision));
+    PQ_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return PQ_OK;
+  }
+  // pageable buffers: device copies of C and sigma stay with the handle (grow-only), so repeated calls
+  // allocate nothing; with ldc == n (and lds == n) each block moves in one copy
   const size_t bytes = sizeof(double) * (size_t)n * nvec + 16;
   PQ_TRY(h->host_c.ensure(bytes));
   PQ_TRY(h->host_s.ensure(bytes));
