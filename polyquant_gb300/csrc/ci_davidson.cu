@@ -109,6 +109,55 @@ __global__ void unit_vectors_kernel(double *V, int64_t n, const int64_t *idx, in
   }
 }
 
+// Selection of the m smallest diagonal elements in the order (value, index), one element per pass: pass j
+// finds the smallest pair above the pair of pass j-1 (block minima, then one block over the block minima).
+constexpr int SEL_BLOCKS = 152 * 4, SEL_THREADS = 256;
+
+struct ValIdx {
+  double v;
+  int64_t i;
+};
+__device__ __forceinline__ bool vi_less(double a, int64_t ia, double b, int64_t ib) { return a < b || (a == b && ia < ib); }
+__device__ __forceinline__ ValIdx vi_min_block(ValIdx x) {
+  __shared__ ValIdx red[SEL_THREADS / 32];
+  for (int o = 16; o; o >>= 1) {
+    const double v = __shfl_xor_sync(0xffffffffu, x.v, o);
+    const int64_t i = __shfl_xor_sync(0xffffffffu, x.i, o);
+    if (vi_less(v, i, x.v, x.i)) x = {v, i};
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    x = threadIdx.x < SEL_THREADS / 32 ? red[threadIdx.x] : ValIdx{INFINITY, INT64_MAX};
+    for (int o = 16; o; o >>= 1) {
+      const double v = __shfl_xor_sync(0xffffffffu, x.v, o);
+      const int64_t i = __shfl_xor_sync(0xffffffffu, x.i, o);
+      if (vi_less(v, i, x.v, x.i)) x = {v, i};
+    }
+  }
+  return x;
+}
+
+// block minima of the pairs (D[i], i) above sel[j - 1] (every pair for j = 0)
+__global__ void __launch_bounds__(SEL_THREADS) select_pass_kernel(const double *D, int64_t n, const ValIdx *sel, int j,
+                                                                  ValIdx *blk) {
+  const ValIdx prev = j > 0 ? sel[j - 1] : ValIdx{-INFINITY, -1};
+  ValIdx best{INFINITY, INT64_MAX};
+  for (int64_t i = (int64_t)blockIdx.x * SEL_THREADS + threadIdx.x; i < n; i += (int64_t)gridDim.x * SEL_THREADS) {
+    const double v = D[i];
+    if (vi_less(prev.v, prev.i, v, i) && vi_less(v, i, best.v, best.i)) best = {v, i};
+  }
+  best = vi_min_block(best);
+  if (threadIdx.x == 0) blk[blockIdx.x] = best;
+}
+__global__ void __launch_bounds__(SEL_THREADS) select_final_kernel(const ValIdx *blk, int nblk, ValIdx *sel, int j) {
+  ValIdx best{INFINITY, INT64_MAX};
+  for (int b = threadIdx.x; b < nblk; b += SEL_THREADS)
+    if (vi_less(blk[b].v, blk[b].i, best.v, best.i)) best = blk[b];
+  best = vi_min_block(best);
+  if (threadIdx.x == 0) sel[j] = best;
+}
+
 // T[:, j] = R[:, j] / (theta_j - D)   (diagonal preconditioner)
 __global__ void precondition_kernel(const double *R, const double *D, const double *theta, int64_t n, int k,
                                     double *T) {
@@ -185,16 +234,23 @@ pq_status DavidsonRun::init(pq_ci_handle *hh, const pq_davidson_params &pp, ::cu
   PQ_TRY(dth.alloc(sizeof(double) * std::max(k, 8)));
   theta.assign(k, 0.0);
   rnorm.assign(k, 0.0);
-  // initial subspace: unit vectors at the m0 smallest diagonal elements
-  std::vector<double> diag(n);
-  PQ_CUDA_TRY(cudaMemcpyAsync(diag.data(), h->d_diag.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
-  PQ_CUDA_TRY(cudaStreamSynchronize(st));
-  std::vector<int64_t> idx(n);
-  std::iota(idx.begin(), idx.end(), 0);
-  auto cmp = [&](int64_t a, int64_t b) { return diag[a] < diag[b] || (diag[a] == diag[b] && a < b); };
-  std::partial_sort(idx.begin(), idx.begin() + m0, idx.end(), cmp);
-  idx.resize(m0);
-  shift = diag[idx[0]];
+  // initial subspace: unit vectors at the m0 smallest diagonal elements (ties by index), selected on the device
+  std::vector<int64_t> idx(m0);
+  {
+    const int nblk = (int)std::min<int64_t>(SEL_BLOCKS, (n + SEL_THREADS - 1) / SEL_THREADS);
+    PQ_TRY(tmp.ensure(sizeof(ValIdx) * (size_t)(nblk + m0)));
+    ValIdx *blk = tmp.as<ValIdx>(), *sel = blk + nblk;
+    for (int j = 0; j < m0; j++) {
+      select_pass_kernel<<<nblk, SEL_THREADS, 0, st>>>(h->d_diag.as<double>(), n, sel, j, blk);
+      select_final_kernel<<<1, SEL_THREADS, 0, st>>>(blk, nblk, sel, j);
+    }
+    PQ_CUDA_TRY(cudaGetLastError());
+    std::vector<ValIdx> hs(m0);
+    PQ_CUDA_TRY(cudaMemcpyAsync(hs.data(), sel, sizeof(ValIdx) * m0, cudaMemcpyDeviceToHost, st));
+    PQ_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int j = 0; j < m0; j++) idx[j] = hs[j].i;
+    shift = hs[0].v;
+  }
   PQ_TRY(upload(didx, idx, st));
   unit_vectors_kernel<<<grid(), 256, 0, st>>>(V.as<double>(), n, didx.as<int64_t>(), m0);
   PQ_CUDA_TRY(cudaGetLastError());
