@@ -455,6 +455,7 @@ pq_status ci_build(pq_ci_handle *h) {
   PQ_CUDA_TRY(cudaStreamSynchronize(st));
   h->fp32_v2 = sigma32_v2_applicable(h) && getenv("PQ_SIGMA32_GATHER") == nullptr;
   h->fp32_tc = h->fp32_v2 && sigma32_tc_applicable(h) && getenv("PQ_SIGMA32_NO_TC") == nullptr;
+  h->fp32_ss = h->fp32_tc && sigma32_ss_applicable(h) && getenv("PQ_SIGMA32_NO_SS") == nullptr;
   return PQ_OK;
 }
 

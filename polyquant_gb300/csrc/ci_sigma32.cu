@@ -10,6 +10,10 @@
 //      (Ja, Ib) of a warp are consecutive in memory.
 //   2. beta-side terms (beta singles, beta-beta doubles): the same kernel on the
 //      transposed copy XT[b][a], result transposed back and added.
+//   For four vectors of a full-CI space whose doubles fill at least 3 % of a
+//   row, the same-spin doubles of both sides are instead dense GEMMs on the
+//   tcgen05 tensor cores (ci_sigma32_ss.cu) and passes 1-2 keep the diagonal
+//   and the singles.
 //   3. alpha-beta doubles: for blocks of four vectors, up to 16 orbitals and
 //      64 alpha singles per string, a GEMM per alpha string on the tcgen05
 //      tensor cores (ci_sigma32_tc.cu).  Otherwise input-stationary on the CUDA cores: CTA
@@ -76,10 +80,14 @@ struct RowSideArgs {
   double shift;
   const float *X;
   float *Y;
+  const float *coul;        // without DOUBLES: [pair_row][col] = sum_{k in occ(col)} (pair_row | kk)
 };
 
 // Row-side terms: CTA per row string, thread per column string.
-template <int NV, bool DIAG>
+// DOUBLES = false leaves the same-spin doubles to the tensor-core GEMMs (ci_sigma32_ss.cu) and takes the
+// singles' opposite-spin Coulomb sums from the precomputed table p.coul (one coalesced load per single
+// instead of a sum over the column string's occupied orbitals).
+template <int NV, bool DIAG, bool DOUBLES>
 __global__ void __launch_bounds__(256) rowside_kernel(RowSideArgs p) {
   extern __shared__ float jrow[];  // [e][k] = (pair_e | kk) for the row string's singles e
   using V = typename FVec<NV>::V;
@@ -89,11 +97,13 @@ __global__ void __launch_bounds__(256) rowside_kernel(RowSideArgs p) {
   const int64_t c = (blockIdx.x / p.nrow) * 256 + threadIdx.x;
   const int64_t e0 = p.s1_off[r];
   const int n1 = (int)(p.s1_off[r + 1] - e0);
-  for (int t = threadIdx.x; t < n1 * p.n_orb; t += 256) {
-    int e = t / p.n_orb, k = t - e * p.n_orb;
-    jrow[t] = p.erc[(int64_t)(p.s1_info[e0 + e] >> 1) * p.npair + idx2s(k, k)];
+  if (DOUBLES) {
+    for (int t = threadIdx.x; t < n1 * p.n_orb; t += 256) {
+      int e = t / p.n_orb, k = t - e * p.n_orb;
+      jrow[t] = p.erc[(int64_t)(p.s1_info[e0 + e] >> 1) * p.npair + idx2s(k, k)];
+    }
+    __syncthreads();
   }
-  __syncthreads();
   if (c >= p.ncol) return;
   const uint64_t mc = p.col_str[c];
   V acc = vzero<V>();
@@ -105,19 +115,25 @@ __global__ void __launch_bounds__(256) rowside_kernel(RowSideArgs p) {
     const int J = __ldg(p.s1_J + e0 + e);
     const int info = __ldg(p.s1_info + e0 + e);
     float h = __ldg(p.s1_F + e0 + e);
-    const float *jr = jrow + e * p.n_orb;
-    uint64_t m = mc;
-    while (m) {
-      int k = __ffsll((long long)m) - 1;
-      h += jr[k];
-      m &= m - 1;
+    if (DOUBLES) {
+      const float *jr = jrow + e * p.n_orb;
+      uint64_t m = mc;
+      while (m) {
+        int k = __ffsll((long long)m) - 1;
+        h += jr[k];
+        m &= m - 1;
+      }
+    } else {
+      h += __ldg(p.coul + (int64_t)(info >> 1) * p.ncol + c);
     }
     vfma(acc, fflip(h, (uint32_t)(info & 1)), FVec<NV>::ld(p.X + ((int64_t)J * p.ncol + c) * NV));
   }
-  const int64_t d0 = p.s2_off[r], d1 = p.s2_off[r + 1];
-  for (int64_t e = d0; e < d1; e++) {
-    const int J = __ldg(p.s2_J + e);
-    vfma(acc, __ldg(p.s2_D + e), FVec<NV>::ld(p.X + ((int64_t)J * p.ncol + c) * NV));
+  if (DOUBLES) {
+    const int64_t d0 = p.s2_off[r], d1 = p.s2_off[r + 1];
+    for (int64_t e = d0; e < d1; e++) {
+      const int J = __ldg(p.s2_J + e);
+      vfma(acc, __ldg(p.s2_D + e), FVec<NV>::ld(p.X + ((int64_t)J * p.ncol + c) * NV));
+    }
   }
   *reinterpret_cast<V *>(p.Y + (r * p.ncol + c) * NV) = acc;
 }
@@ -275,6 +291,10 @@ static pq_status sigma32_v2_impl(pq_ci_handle *h, const float *X, float *Y, doub
   vtranspose_kernel<NV, false><<<dim3((unsigned)((nb + 31) / 32), (unsigned)((na + 31) / 32)), tb, 0, st>>>(X, na, nb, XT);
   PQ_CUDA_TRY(cudaGetLastError());
   // 2. alpha side (with the diagonal) -> Y
+  // same-spin doubles on the tensor cores (4 roots, full CI) or in the row-side gathers
+  const bool ss = NV == 4 && h->fp32_ss;
+  const bool doubles = !ss;
+  if (ss) PQ_TRY(ci_sigma32_ss_prepare(h));
   auto rowside = [&](int spin_row, const float *src, float *dst, const float *erc, bool diag) -> pq_status {
     const SpinTablesDev &tr = h->tab[0][spin_row];
     const SpinTablesDev &tc = h->tab[0][1 - spin_row];
@@ -298,12 +318,17 @@ static pq_status sigma32_v2_impl(pq_ci_handle *h, const float *X, float *Y, doub
     a.shift = shift;
     a.X = src;
     a.Y = dst;
-    const size_t smem = sizeof(float) * (size_t)std::max(tr.max1, 1) * n_orb;
+    a.coul = ss ? ci_sigma32_ss_coulomb(h, spin_row) : nullptr;
+    const size_t smem = doubles ? sizeof(float) * (size_t)std::max(tr.max1, 1) * n_orb : 0;
     const int64_t grid = a.nrow * a.nblk;
-    if (diag)
-      rowside_kernel<NV, true><<<(unsigned)grid, 256, smem, st>>>(a);
+    if (diag && doubles)
+      rowside_kernel<NV, true, true><<<(unsigned)grid, 256, smem, st>>>(a);
+    else if (diag)
+      rowside_kernel<NV, true, false><<<(unsigned)grid, 256, smem, st>>>(a);
+    else if (doubles)
+      rowside_kernel<NV, false, true><<<(unsigned)grid, 256, smem, st>>>(a);
     else
-      rowside_kernel<NV, false><<<(unsigned)grid, 256, smem, st>>>(a);
+      rowside_kernel<NV, false, false><<<(unsigned)grid, 256, smem, st>>>(a);
     PQ_CUDA_TRY(cudaGetLastError());
     return PQ_OK;
   };
@@ -313,6 +338,7 @@ static pq_status sigma32_v2_impl(pq_ci_handle *h, const float *X, float *Y, doub
   // 4. Y[a][b] += ZT[b][a]
   vtranspose_kernel<NV, true><<<dim3((unsigned)((na + 31) / 32), (unsigned)((nb + 31) / 32)), tb, 0, st>>>(ZT, nb, na, Y);
   PQ_CUDA_TRY(cudaGetLastError());
+  if (ss) PQ_TRY(ci_sigma32_same_spin_tc(h, X, Y));
   // 5. alpha-beta doubles: on the tensor cores where the shape allows (ci_sigma32_tc.cu), else
   // scattered with vector atomics
   if (h->fp32_tc && NV == 4) return ci_sigma32_ab_tc(h, X, Y, NV);

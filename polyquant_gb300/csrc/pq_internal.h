@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include <chrono>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -76,6 +77,9 @@ struct SpinTablesDev {
   DevBuf e_same64;         // per-string same-spin energy (diagonal part)
 };
 
+struct SameSpinGemm;  // ci_sigma32_ss.cu
+void ss_delete(SameSpinGemm *g);
+
 }  // namespace pq
 
 struct pq_ci_handle {
@@ -115,6 +119,8 @@ struct pq_ci_handle {
   int tc_sms = 0;
   bool tc_ready = false;
   bool fp32_tc = false;  // the FP32 full-CI sigma uses the tensor-core alpha-beta path
+  bool fp32_ss = false;  // ... and the same-spin doubles as tensor-core GEMMs (ci_sigma32_ss.cu)
+  std::unique_ptr<pq::SameSpinGemm, void (*)(pq::SameSpinGemm *)> ss{nullptr, pq::ss_delete};
   // two species: addressing of the product space (see ci_two.cu)
   std::vector<int32_t> e_a, e_b;        // species-0 (alpha, beta) string pair of each kept pair ie
   std::vector<int64_t> ebase;           // first determinant of pair ie's species-1 block
@@ -174,6 +180,11 @@ pq_status ci_sigma32_v2(pq_ci_handle *h, const void *X, void *Y, int nvp, double
 // ci_sigma32_tc.cu: Y += alpha-beta doubles of X (FP32, interleaved), on the tensor cores
 bool sigma32_tc_applicable(const pq_ci_handle *h);
 pq_status ci_sigma32_ab_tc(pq_ci_handle *h, const void *X, void *Y, int nvp);
+// ci_sigma32_ss.cu
+bool sigma32_ss_applicable(const pq_ci_handle *h);
+pq_status ci_sigma32_same_spin_tc(pq_ci_handle *h, const float *X, float *Y);
+pq_status ci_sigma32_ss_prepare(pq_ci_handle *h);
+const float *ci_sigma32_ss_coulomb(const pq_ci_handle *h, int spin_row);
 pq_status ci_to_il(pq_ci_handle *h, const double *C, int64_t ldc, int v0, int nv, int nvp, int precision, void *X);
 pq_status ci_from_il(pq_ci_handle *h, const void *Y, int v0, int nv, int nvp, int precision, double *S, int64_t lds);
 // ci_davidson.cu

@@ -182,6 +182,39 @@ def test_sigma_fp32_tensor_core_alpha_beta_matches_scatter_path(monkeypatch, sha
     g_sc.close()
 
 
+@pytest.mark.parametrize("shape", [(12, 6, 6, True), (13, 6, 5, True), (12, 6, 6, False)])
+def test_sigma_fp32_same_spin_gemm_matches_gather_path(monkeypatch, shape):
+    """The FP32 full-CI sigma with both same-spin double blocks as dense tensor-core GEMMs (FP16 hi/lo split,
+    FP32 accumulation; 3 and 4 vectors use the 4-wide block) against the same sigma with the row-side gathers
+    (PQ_SIGMA32_NO_SS, read when a handle is created) and against FP64: equal spin lists (the beta GEMM reuses
+    the alpha matrix), unequal lists, and unrestricted integrals (two matrices); partial tiles in M, N and K."""
+    from polyquant_gb300._lib import PQ_FP32
+
+    n, a, b, restricted = shape
+    p = synthetic_fci(n, a, b, seed=40 + n) if restricted else synthetic_unrestricted(n, a, b, seed=41)
+    g_ss = gpu_detset(p)
+    monkeypatch.setenv("PQ_SIGMA32_NO_SS", "1")
+    g_ga = gpu_detset(p)
+    monkeypatch.delenv("PQ_SIGMA32_NO_SS")
+    gen = torch.Generator(device="cuda").manual_seed(n + a)
+    for k in (4, 3):
+        X = torch.randn(g_ss.N_dets, k, device="cuda", dtype=torch.float64, generator=gen)
+        S64 = g_ss.sigma(X)
+        S_ss = g_ss.sigma(X, precision=PQ_FP32)
+        S_ga = g_ga.sigma(X, precision=PQ_FP32)
+        scale = S64.abs().max().item()
+        assert (S_ss - S64).abs().max().item() <= SIGMA_RTOL_FP32 * scale
+        assert (S_ga - S64).abs().max().item() <= SIGMA_RTOL_FP32 * scale
+        assert (S_ss - S64).abs().max().item() <= 10 * max((S_ga - S64).abs().max().item(), 1e-7 * scale)
+    for f in (1e-30, 1e20):
+        X = f * torch.randn(g_ss.N_dets, 4, device="cuda", dtype=torch.float64, generator=gen)
+        S64 = g_ss.sigma(X)
+        S_ss = g_ss.sigma(X, precision=PQ_FP32)
+        assert (S_ss - S64).abs().max().item() <= SIGMA_RTOL_FP32 * S64.abs().max().item()
+    g_ss.close()
+    g_ga.close()
+
+
 def test_davidson_h2o_energies(cases, h2o):
     """H2O/STO-3G CISD energies (calculation_test.cpp:253-260) and FCI vs the oracle's dense H."""
     r = h2o("library")
