@@ -16,20 +16,21 @@
 //   warp 0      TMEM owner and MMA issuer (M = 128 rows (Jb, v), N = 128
 //               pairs, K = 64 singles; hi*hi + hi*lo + lo*hi in FP16 with FP32
 //               accumulation; two accumulators so the epilogue overlaps);
-//   warps 1-4   converters, thread <-> operand row: each thread copies its own
-//               column of the 64 gathered rows of a 128-value tile into a
-//               shared stage with 4-byte asynchronous copies, one tile ahead,
-//               then scales it, splits it into FP16 hi/lo and writes the
-//               K-major 128-byte-swizzled operand tile (two stages); they also
-//               build B per alpha string from the cross-spin integrals (two
-//               buffers, so the next string's B is ready before its tiles);
-//   warps 5-8   epilogue: tcgen05.ld of the accumulator; per 32-column chunk a
-//               warp parks its values in its own shared block and reads them
-//               back so that each lane holds the four roots of one (Jb, q),
-//               then adds them to sigma(Ia, target) with one vector reduction
-//               (red.global.add.v4.f32); the [Jb][q] scatter-table rows of the
-//               next tile arrive in shared memory by asynchronous copies while
-//               the MMAs run.
+//   warps 1-4   converters: thread (c, kq) owns beta string c of a 32-string tile
+//               (operand rows 4c .. 4c + 3) and alpha singles 16 kq .. 16 kq + 15;
+//               it copies the 16-byte vectors X[Ja][Jb][0..3] of its singles into a
+//               shared stage with asynchronous copies, one tile ahead, then scales
+//               them, splits them into FP16 hi/lo and writes its part of the K-major
+//               128-byte-swizzled operand tile (two stages); they also build B per
+//               alpha string from the cross-spin integrals (one buffer);
+//   warps 5-8   epilogue: tcgen05.ld of the accumulator into a shared staging copy
+//               of the whole tile ([Jb][q][v]), which frees the accumulator at once;
+//   warps 5-11  then each thread takes targets from the tile's precomputed scatter
+//               list (the distinct Ib reached from the tile's 32 beta strings, each
+//               with its (Jb, q, phase) contributions: 2.1 per target at 16
+//               orbitals), sums them and adds the sum into sigma(Ia, Ib) with one
+//               vector reduction (red.global.add.v4.f32).  Staging full / empty are
+//               mbarriers, so every wait in the kernel is bounded.
 // A CTA is the only writer of its sigma rows, so the reductions never contend
 // between CTAs.  On this GPU a shared-memory float atomic adds fewer values
 // per clock than a global vector reduction, which carries all four roots.
@@ -46,6 +47,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <utility>
+#include <vector>
 
 #include "pq_internal.h"
 
@@ -57,28 +60,26 @@ constexpr int BN = 128;       // off-diagonal beta pairs (TMEM columns per accum
 constexpr int BK = 64;        // alpha singles (K), one 128-byte swizzle span of FP16
 constexpr int NV = 4;         // roots per determinant (interleaved); other widths use the CUDA-core path
 constexpr int ASTAGES = 2;    // A operand stages
+constexpr int TJB = BM / NV;  // beta strings per tile (32)
 constexpr int OP_TILE = BM * BK * 2;          // 16 KB: one FP16 operand tile (A or B)
 constexpr int RAW_TILE = BK * BM * 4;         // 32 KB: the gathered FP32 rows of one tile
-constexpr int WROWS = BM / NV / 4;            // beta strings per epilogue warp and tile (8)
-// scatter-table row in shared memory (uint16): 272 bytes, a multiple of the 16-byte copies that fill it, and
-// 68 words apart so the eight rows a warp reads fall in different banks
-constexpr int TROW = 136;
-constexpr int TAB_STAGE = 4 * WROWS * TROW * 2;  // bytes: one tile's table rows (32 beta strings), 8.5 KB
-constexpr int STG_WARP = WROWS * 32 * NV;        // floats: one warp's 8 beta strings x 32 columns x 4 roots
-constexpr int NTHREADS = 288;                    // 9 warps
-constexpr int CONV0 = 1, EPI0 = 5;               // first converter / epilogue warp
+constexpr int STG_BYTES = TJB * BN * NV * 4;  // 64 KB: the whole accumulator tile, [Jb][q][v]
+constexpr int KQ = BK / 4;                    // alpha singles per converter thread (16)
+constexpr int NPRE = 6;                       // scatter-list entries per processing thread loaded ahead of a tile
+constexpr int NTHREADS = 384;                    // 12 warps
+constexpr int CONV0 = 1, EPI0 = 5, PROC0 = 9;    // first converter / epilogue (staging) / list-only warp
+constexpr int NPROC = (NTHREADS / 32 - EPI0) * 32;  // threads that process the scatter lists (224)
 constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
-// shared memory: A hi/lo x ASTAGES, B hi/lo x 2, raw rows x 2, table rows x 2, epilogue staging x 4 warps,
-// per-warp alpha partner lists, barriers
-constexpr int SMEM_OPS = ASTAGES * 2 * OP_TILE + 2 * 2 * OP_TILE + 2 * RAW_TILE + 2 * TAB_STAGE + 4 * STG_WARP * 4;
-constexpr int NBARS = 2 * ASTAGES + 9;           // a_full, a_empty, acc_full/empty, b_full/empty, drain
+// shared memory: A hi/lo x ASTAGES, B hi/lo (one buffer), raw rows x 2, accumulator staging, per-warp alpha
+// partner lists, barriers
+constexpr int SMEM_OPS = ASTAGES * 2 * OP_TILE + 2 * OP_TILE + 2 * RAW_TILE + STG_BYTES;
+constexpr int NBARS = 2 * ASTAGES + 9;  // a_full, a_empty, acc_full[2], acc_empty[2], b_full, b_empty, drain,
+                                        // stg_full, stg_empty
 constexpr int SMEM_BYTES = SMEM_OPS + 4 * BK * 2 + 1024 + NBARS * 8 + 16;
-static_assert((TROW * 2) % 16 == 0 && TAB_STAGE % 16 == 0 && (WROWS * TROW * 2) % 16 == 0,
-              "16-byte copies into the table stage need 16-byte aligned rows");
-static_assert((2 * RAW_TILE + 2 * TAB_STAGE) % 16 == 0, "the epilogue staging is read as float4");
+static_assert(SMEM_OPS % 16 == 0 && (2 * RAW_TILE) % 16 == 0, "16-byte alignment of the copy and staging areas");
 static_assert(SMEM_BYTES <= 232448, "shared memory per CTA");
 
-enum { ERR_AEMPTY = 2, ERR_AFULL = 3, ERR_ACC = 4, ERR_B = 5 };
+enum { ERR_AEMPTY = 2, ERR_AFULL = 3, ERR_ACC = 4, ERR_B = 5, ERR_STG = 6 };
 
 struct Args {
   const float *X;          // [na][nb][NV] interleaved input (FP32)
@@ -91,7 +92,11 @@ struct Args {
   const float *eab;        // (pair_alpha | pair_beta) row-major FP32
   int npair, n_off;        // beta pairs: all, off-diagonal (<= BN)
   float sw;                // power-of-two scale of the integrals
-  const uint16_t *btab;    // [nb][BN]: (Ib << 1 | phase) of the single of Jb through pair q, or 0xFFFF
+  // scatter lists per tile of 32 beta strings: entries t_off[t] .. t_off[t + 1] of tile t, each
+  // {Ib | n << 16, up to six contributions as uint16 pairs}; a contribution is (phase << 12 | jb_local << 7 | q)
+  // (a target with more than six contributions takes several entries)
+  const int32_t *t_off;
+  const int4 *tent;
   long long wait_cycles;
   int *err;
   long long *prof;         // per-CTA role timers (PQ_ABTC_PROFILE builds only)
@@ -205,6 +210,25 @@ __device__ __forceinline__ void store_row(unsigned char *th, unsigned char *tl, 
   }
 }
 
+// 16 K values (alpha singles 16 kq .. 16 kq + 15) of row r -> the two 16-byte chunks 2 kq, 2 kq + 1 of the
+// FP16 hi/lo tiles (same swizzled layout as store_row)
+__device__ __forceinline__ void store_quarter(unsigned char *th, unsigned char *tl, int r, int kq, const float (&x)[KQ]) {
+#pragma unroll
+  for (int hh = 0; hh < 2; hh++) {
+    const int ch = 2 * kq + hh;
+    __half2 h[4], l[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const float a = x[hh * 8 + 2 * e], b = x[hh * 8 + 2 * e + 1];
+      h[e] = __floats2half2_rn(a, b);
+      const float2 f = __half22float2(h[e]);
+      l[e] = __floats2half2_rn(a - f.x, b - f.y);
+    }
+    *reinterpret_cast<uint4 *>(th + r * 128 + ((ch ^ (r & 7)) << 4)) = *reinterpret_cast<const uint4 *>(h);
+    *reinterpret_cast<uint4 *>(tl + r * 128 + ((ch ^ (r & 7)) << 4)) = *reinterpret_cast<const uint4 *>(l);
+  }
+}
+
 // power of two 2^e with x * 2^e in [2^14, 2^15) (1 for x == 0)
 __device__ __forceinline__ float fp16_scale(float x) {
   if (!(x > 0.0f) || !isfinite(x)) return 1.0f;
@@ -216,18 +240,18 @@ __device__ __forceinline__ float fp16_scale(float x) {
 __global__ void __launch_bounds__(NTHREADS, 1) ab_tc_kernel(Args g) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
-  unsigned char *a_hi = smem;                                       // [ASTAGES] x 16 KB
-  unsigned char *a_lo = a_hi + ASTAGES * OP_TILE;                   // [ASTAGES] x 16 KB
-  unsigned char *b_hi = a_lo + ASTAGES * OP_TILE;                   // [2] x 16 KB
-  unsigned char *b_lo = b_hi + 2 * OP_TILE;                         // [2] x 16 KB
-  float *raw = reinterpret_cast<float *>(b_lo + 2 * OP_TILE);       // [2][BK][BM]
-  uint16_t *tab = reinterpret_cast<uint16_t *>(raw + 2 * BK * BM);  // [2][4 warps][WROWS][TROW]
-  float *stg_all = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(tab) + 2 * TAB_STAGE);  // [4][STG_WARP]
-  uint16_t *ja_all = reinterpret_cast<uint16_t *>(stg_all + 4 * STG_WARP);  // [4][BK] alpha partner strings
+  unsigned char *a_hi = smem;                                  // [ASTAGES] x 16 KB
+  unsigned char *a_lo = a_hi + ASTAGES * OP_TILE;              // [ASTAGES] x 16 KB
+  unsigned char *b_hi = a_lo + ASTAGES * OP_TILE;              // 16 KB
+  unsigned char *b_lo = b_hi + OP_TILE;                        // 16 KB
+  float *raw = reinterpret_cast<float *>(b_lo + OP_TILE);      // [2][BK][BM]
+  float *stg = raw + 2 * BK * BM;                              // [TJB][BN][NV], column swizzled by the row
+  uint16_t *ja_all = reinterpret_cast<uint16_t *>(reinterpret_cast<unsigned char *>(stg) + STG_BYTES);  // [4][BK]
   uint64_t *bars = reinterpret_cast<uint64_t *>(ja_all + 4 * BK);
   uint64_t *a_full = bars, *a_empty = bars + ASTAGES, *acc_full = bars + 2 * ASTAGES;
-  uint64_t *acc_empty = acc_full + 2, *b_full = acc_full + 4, *b_empty = acc_full + 6, *drain = acc_full + 8;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
+  uint64_t *acc_empty = acc_full + 2, *b_full = acc_full + 4, *b_empty = acc_full + 5, *drain = acc_full + 6;
+  uint64_t *stg_full = acc_full + 7, *stg_empty = acc_full + 8;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(stg_empty + 1);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -243,10 +267,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) ab_tc_kernel(Args g) {
     for (int s = 0; s < 2; s++) {
       mbar_init(smem_u32(acc_full + s), 1);
       mbar_init(smem_u32(acc_empty + s), 4);
-      mbar_init(smem_u32(b_full + s), 4);
-      mbar_init(smem_u32(b_empty + s), 1);
     }
+    mbar_init(smem_u32(b_full), 4);
+    mbar_init(smem_u32(b_empty), 1);
     mbar_init(smem_u32(drain), 1);
+    mbar_init(smem_u32(stg_full), 4);
+    mbar_init(smem_u32(stg_empty), NPROC / 32);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -268,15 +294,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) ab_tc_kernel(Args g) {
       int seq = 0, grp = 0;
       bool ok = true;
       for (int64_t ia = blockIdx.x; ia < g.na && ok && !*abort_flag; ia += gridDim.x, grp++) {
-        const int bb = grp & 1;
         PT(tb0);
-        if (!mbar_wait(smem_u32(b_full + bb), (uint32_t)((grp >> 1) & 1), g.wait_cycles)) {
+        if (!mbar_wait(smem_u32(b_full), (uint32_t)(grp & 1), g.wait_cycles)) {
           atomicCAS(g.err, 0, ERR_B);
           ok = false;
           break;
         }
         PACC(3, tb0);
-        const uint32_t bh = smem_u32(b_hi + bb * OP_TILE), bl = smem_u32(b_lo + bb * OP_TILE);
+        const uint32_t bh = smem_u32(b_hi), bl = smem_u32(b_lo);
         for (int t = 0; t < mt; t++, seq++) {
           const int s = seq % ASTAGES, a = seq & 1;
           const uint32_t ps = (uint32_t)((seq / ASTAGES) & 1), pa = (uint32_t)((seq >> 1) & 1);
@@ -312,7 +337,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) ab_tc_kernel(Args g) {
           mma_commit(smem_u32(acc_full + a));
         }
         if (!ok) break;
-        mma_commit(smem_u32(b_empty + bb));  // B of this alpha string is free once its MMAs completed
+        mma_commit(smem_u32(b_empty));  // B of this alpha string is free once its MMAs completed
       }
       if (!ok) *abort_flag = 1;
       // every MMA issued here has completed before TMEM is freed
@@ -321,9 +346,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) ab_tc_kernel(Args g) {
     }
     __syncwarp();
   } else if (warp < EPI0) {
-    // ---- converters: thread <-> operand row (A: element e of the tile, B: off-diagonal beta pair)
-    const int r = threadIdx.x - 32 * CONV0;     // 0..127
-    uint16_t *ja = ja_all + (warp - CONV0) * BK;  // this warp's copy of the alpha partner list
+    // ---- converters.  A: thread (c = lane, kq = warp - CONV0) owns beta string c of the tile (its four
+    // operand rows 4c .. 4c + 3) and alpha singles 16 kq .. 16 kq + 15: it copies the 16-byte vectors
+    // X[Ja(k)][Jb][0..3] of its singles into the raw stage, one tile ahead, and converts only what it copied
+    // (no cross-thread wait).  B: thread r = 32 kq + c owns the off-diagonal beta pair q = r.
+    const int kq = warp - CONV0, c = lane;
+    const int r = threadIdx.x - 32 * CONV0;       // 0..127
+    uint16_t *ja = ja_all + kq * BK;              // this warp's copy of the alpha partner list
     const float sx = fp16_scale(*g.xmax);
     int seq = 0, grp = 0;
     bool stop = false;
@@ -337,9 +366,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) ab_tc_kernel(Args g) {
       ja[lane] = (uint16_t)(lane < n1 ? g.a_J[base + lane] : 0);
       ja[lane + 32] = (uint16_t)(lane + 32 < n1 ? g.a_J[base + lane + 32] : 0);
       __syncwarp();
-      const int bb = grp & 1;
       PT(cb0);
-      if (!warp_wait(smem_u32(b_empty + bb), (uint32_t)((grp >> 1) & 1) ^ 1u, g.wait_cycles)) {
+      if (!warp_wait(smem_u32(b_empty), (uint32_t)(grp & 1) ^ 1u, g.wait_cycles)) {
         if (lane == 0) atomicCAS(g.err, 0, ERR_B);
         *abort_flag = 1;
         break;
@@ -359,20 +387,22 @@ __global__ void __launch_bounds__(NTHREADS, 1) ab_tc_kernel(Args g) {
             w[k] = (info & 1) ? -x : x;
           }
         }
-        store_row(b_hi + bb * OP_TILE, b_lo + bb * OP_TILE, r, w);
+        store_row(b_hi, b_lo, r, w);
       }
       PACC(6, cb1);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncwarp();
-      if (lane == 0) mbar_arrive(smem_u32(b_full + bb));
-      // A tiles: each thread copies its own column of the 64 gathered rows into the raw stage with 4-byte
-      // asynchronous copies, one tile ahead, and converts only what it copied (no cross-thread wait)
+      if (lane == 0) mbar_arrive(smem_u32(b_full));
       auto issue = [&](int t, int stage) {
-        const int64_t e = (int64_t)t * BM + r;
+        const int64_t e = (int64_t)t * BM + 4 * c;  // first float of beta string c of tile t in an alpha row
         if (e < row_len) {
           const float *col = g.X + e;
-          const uint32_t dst = smem_u32(raw + stage * BK * BM + r);
-          for (int k = 0; k < n1; k++) cp_async4(dst + k * BM * 4, col + (int64_t)ja[k] * row_len);
+          const uint32_t dst = smem_u32(raw + stage * BK * BM + 4 * c);
+#pragma unroll 4
+          for (int j = 0; j < KQ; j++) {
+            const int k = kq * KQ + j;
+            if (k < n1) cp_async16(dst + k * BM * 4, col + (int64_t)ja[k] * row_len);
+          }
         }
         cp_commit();
       };
@@ -403,12 +433,21 @@ __global__ void __launch_bounds__(NTHREADS, 1) ab_tc_kernel(Args g) {
         PACC(9, cc0);
         PT(cs0);
         {
-          const bool in = (int64_t)t * BM + r < row_len;
-          const float *src = raw + (seq & 1) * BK * BM + r;
-          float x[BK];
+          const bool in = (int64_t)t * BM + 4 * c < row_len;
+          const float *src = raw + (seq & 1) * BK * BM + 4 * c;
+          float x[NV][KQ];
 #pragma unroll
-          for (int k = 0; k < BK; k++) x[k] = (in && k < n1) ? src[k * BM] * sx : 0.0f;
-          store_row(a_hi + s * OP_TILE, a_lo + s * OP_TILE, r, x);
+          for (int j = 0; j < KQ; j++) {
+            const int k = kq * KQ + j;
+            float4 v4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (in && k < n1) v4 = *reinterpret_cast<const float4 *>(src + k * BM);
+            x[0][j] = v4.x * sx;
+            x[1][j] = v4.y * sx;
+            x[2][j] = v4.z * sx;
+            x[3][j] = v4.w * sx;
+          }
+#pragma unroll
+          for (int v = 0; v < NV; v++) store_quarter(a_hi + s * OP_TILE, a_lo + s * OP_TILE, 4 * c + v, kq, x[v]);
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncwarp();
@@ -420,86 +459,107 @@ __global__ void __launch_bounds__(NTHREADS, 1) ab_tc_kernel(Args g) {
       __syncwarp();
     }
   } else {
-    // ---- epilogue: accumulator -> vector reductions into sigma(Ia, target, 0..3).  Each warp stages and
-    // reads back only its own 32 TMEM lanes (8 beta strings x 4 roots), so the warps never wait on each other.
-    const int q = warp & 3;  // TMEM lane quadrant of this warp
+    // ---- epilogue.  Per tile: warps EPI0 .. EPI0 + 3 copy the accumulator into the staging area ([Jb][q][v],
+    // the column swizzled by the row) and release the accumulator; then they and the list-only warps
+    // PROC0 .. take targets of the tile's scatter list, sum their contributions from the staging area and
+    // add each sum into sigma(Ia, target) with one vector reduction.  Staging full / empty are mbarriers
+    // with bounded waits.
+    const bool stager = warp < PROC0;
+    const int q4 = warp & 3;                 // TMEM lane quadrant of a staging warp
+    const int te = threadIdx.x - 32 * EPI0;  // 0 .. NPROC - 1
     int seq = 0;
     bool dead = false;
     // the two inverse scales are powers of two inside the FP32 range, and so is their product
     const float unscale = (1.0f / g.sw) * (1.0f / fp16_scale(*g.xmax));
-    uint16_t *my_tab = tab + q * WROWS * TROW;  // this warp's 8 rows inside a table stage
-    float *stg = stg_all + q * STG_WARP;
-    // scatter-table rows of this warp's 8 beta strings of tile t -> table stage (16-byte copies, 4 per lane)
-    auto issue = [&](int t, int stage) {
-      const int64_t jb0 = ((int64_t)t * BM + q * 32) / NV;  // first beta string of this warp's rows
-      const uint32_t base = smem_u32(my_tab + stage * (TAB_STAGE / 2));
-#pragma unroll
-      for (int i = 0; i < 4; i++) {
-        const int piece = lane + 32 * i;  // 8 rows x 16 pieces of 16 bytes
-        const int row = piece >> 4, pc = piece & 15;
-        if ((jb0 + row) * NV < row_len) cp_async16(base + row * TROW * 2 + pc * 16, g.btab + (jb0 + row) * BN + pc * 8);
-      }
-      cp_commit();
-    };
-    issue(0, seq & 1);
+    const int jl = 8 * q4 + (lane >> 2), vv = lane & 3;  // a staging lane's accumulator row (beta string, root)
     for (int64_t ia = blockIdx.x; ia < g.na; ia += gridDim.x) {
       float *yrow = g.Y + ia * row_len;
       for (int t = 0; t < mt; t++, seq++) {
         if (dead) continue;
-        issue(t + 1 < mt ? t + 1 : 0, (seq + 1) & 1);  // the next tile's rows load while this tile waits
-        const int a = seq & 1;
-        const uint32_t pa = (uint32_t)((seq >> 1) & 1);
+        // this tile's first NPRE list entries per thread: the loads do not depend on the accumulator, so
+        // their latency overlaps the wait for it and the staging
+        const int k0 = g.t_off[t], k1 = g.t_off[t + 1];
+        int4 pre[NPRE];
+#pragma unroll
+        for (int i = 0; i < NPRE; i++) {
+          const int k = k0 + te + NPROC * i;
+          pre[i] = k < k1 ? __ldg(g.tent + k) : make_int4(0, 0, 0, 0);
+        }
         PT(ew0);
-        if (!warp_wait(smem_u32(acc_full + a), pa, g.wait_cycles)) {
-          if (lane == 0) atomicCAS(g.err, 0, ERR_ACC);
+        if (stager) {
+          const int a = seq & 1;
+          const uint32_t pa = (uint32_t)((seq >> 1) & 1);
+          bool ok = warp_wait(smem_u32(acc_full + a), pa, g.wait_cycles);
+          ok = ok && warp_wait(smem_u32(stg_empty), (uint32_t)(seq & 1) ^ 1u, g.wait_cycles);
+          if (!ok || warp_aborted(abort_flag)) {
+            if (!ok && lane == 0) atomicCAS(g.err, 0, ERR_STG);
+            *abort_flag = 1;
+            dead = true;
+            continue;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t taddr = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(a * BN);
+          float *srow = stg + (int64_t)jl * BN * NV + vv;
+#pragma unroll 1
+          for (int c0 = 0; c0 < BN; c0 += 32) {
+            float d[32];
+            tmem_ld32(taddr + c0, d);
+#pragma unroll
+            for (int j = 0; j < 32; j++) srow[((c0 + j) ^ (jl & 7)) * NV] = d[j];
+          }
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) {
+            mbar_arrive(smem_u32(acc_empty + a));  // the MMAs may refill this accumulator
+            mbar_arrive(smem_u32(stg_full));
+          }
+        }
+        PACC(11, ew0);
+        PT(es0);
+        if (!warp_wait(smem_u32(stg_full), (uint32_t)(seq & 1), g.wait_cycles) || warp_aborted(abort_flag)) {
+          if (lane == 0) atomicCAS(g.err, 0, ERR_STG);
           *abort_flag = 1;
           dead = true;
           continue;
         }
-        if (warp_aborted(abort_flag)) {
-          dead = true;
-          continue;
-        }
-        cp_wait<1>();
-        __syncwarp();
-        PACC(11, ew0);
-        PT(es0);
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * BN);
-        // per 32-column chunk: lane (row rr = lane / 4, root vv = lane % 4) parks its values in the warp's
-        // staging block (column swizzled by the row: conflict-free), then lane c takes column c of each of
-        // the warp's 8 beta strings with its four roots and adds them with one vector reduction
-        const int64_t jb0 = ((int64_t)t * BM + q * 32) / NV;
-        const int rr = lane / NV, vv = lane % NV;
-        const uint16_t *trow = my_tab + (seq & 1) * (TAB_STAGE / 2);
-#pragma unroll 1
-        for (int c0 = 0; c0 < BN; c0 += 32) {
-          float d[32];
-          tmem_ld32(taddr + c0, d);
+        // one entry: sum its contributions from the staging area, one vector reduction into sigma
+        auto apply = [&](const int4 &ent) {
+          const int n = ent.x >> 16;
+          if (n == 0) return;
+          const uint32_t w3[3] = {(uint32_t)ent.y, (uint32_t)ent.z, (uint32_t)ent.w};
+          float4 sm = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-          for (int j = 0; j < 32; j++) stg[(rr * 32 + (j ^ rr)) * NV + vv] = d[j];
-          __syncwarp();
-#pragma unroll
-          for (int i = 0; i < WROWS; i++) {
-            const bool live = (jb0 + i) * NV < row_len;
-            const uint32_t en = live ? trow[i * TROW + c0 + lane] : 0xFFFFu;
-            if (en != 0xFFFFu) {
-              const float4 x = *reinterpret_cast<const float4 *>(stg + (i * 32 + (lane ^ i)) * NV);
-              const float f = (en & 1) ? -unscale : unscale;
-              asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(yrow + (int64_t)(en >> 1) * NV),
-                           "f"(x.x * f), "f"(x.y * f), "f"(x.z * f), "f"(x.w * f)
-                           : "memory");
+          for (int u = 0; u < 6; u++) {
+            if (u < n) {
+              const uint32_t en = (w3[u >> 1] >> (16 * (u & 1))) & 0xFFFFu;
+              const int rl = (int)((en >> 7) & 31), qq = (int)(en & 127);
+              const float4 x = *reinterpret_cast<const float4 *>(stg + ((int64_t)rl * BN + (qq ^ (rl & 7))) * NV);
+              const float f = (en & 4096u) ? -1.0f : 1.0f;
+              sm.x = fmaf(f, x.x, sm.x);
+              sm.y = fmaf(f, x.y, sm.y);
+              sm.z = fmaf(f, x.z, sm.z);
+              sm.w = fmaf(f, x.w, sm.w);
             }
           }
-          __syncwarp();
+          asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(yrow + (int64_t)(ent.x & 0xFFFF) * NV),
+                       "f"(sm.x * unscale), "f"(sm.y * unscale), "f"(sm.z * unscale), "f"(sm.w * unscale)
+                       : "memory");
+        };
+#pragma unroll
+        for (int i = 0; i < NPRE; i++) apply(pre[i]);
+        // the rest of the tile's entries (tiles with more than NPRE x NPROC), four loads at a time
+        for (int kb = k0 + te + NPROC * NPRE; kb < k1; kb += 4 * NPROC) {
+          int4 ent[4];
+#pragma unroll
+          for (int i = 0; i < 4; i++) ent[i] = kb + NPROC * i < k1 ? __ldg(g.tent + kb + NPROC * i) : make_int4(0, 0, 0, 0);
+#pragma unroll
+          for (int i = 0; i < 4; i++) apply(ent[i]);
         }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncwarp();
-        if (lane == 0) mbar_arrive(smem_u32(acc_empty + a));
+        if (lane == 0) mbar_arrive(smem_u32(stg_empty));
         PACC(12, es0);
       }
     }
-    cp_wait<0>();
   }
 #ifdef PQ_ABTC_PROFILE
   {
@@ -573,6 +633,50 @@ static pq_status ab_tc_impl(pq_ci_handle *h, const float *X, float *Y) {
     btab_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, st>>>(tb.s1_off.as<int64_t>(), tb.s1_J.as<int32_t>(),
                                                             tb.s1_info.as<int32_t>(), nb, h->tc_btab.as<uint16_t>());
     PQ_CUDA_TRY(cudaGetLastError());
+    // scatter lists per tile of TJB beta strings: the distinct targets of the tile's (Jb, q) entries, each
+    // with its contributions, so the epilogue issues one reduction per target instead of one per entry
+    {
+      std::vector<uint16_t> bt((size_t)BN * nb);
+      PQ_CUDA_TRY(cudaMemcpyAsync(bt.data(), h->tc_btab.ptr, sizeof(uint16_t) * bt.size(), cudaMemcpyDeviceToHost, st));
+      PQ_CUDA_TRY(cudaStreamSynchronize(st));
+      const int tiles = (int)((nb + TJB - 1) / TJB);
+      std::vector<int32_t> toff(tiles + 1, 0);
+      std::vector<int4> tent;
+      std::vector<std::pair<int32_t, uint16_t>> items;
+      for (int t = 0; t < tiles; t++) {
+        items.clear();
+        for (int jl = 0; jl < TJB && (int64_t)t * TJB + jl < nb; jl++) {
+          const uint16_t *row = bt.data() + ((int64_t)t * TJB + jl) * BN;
+          for (int q = 0; q < BN; q++)
+            if (row[q] != 0xFFFFu)
+              items.push_back({(int32_t)(row[q] >> 1), (uint16_t)(((row[q] & 1u) << 12) | ((unsigned)jl << 7) | (unsigned)q)});
+        }
+        std::sort(items.begin(), items.end());
+        for (size_t u = 0; u < items.size();) {
+          size_t w = u;
+          while (w < items.size() && items[w].first == items[u].first) w++;
+          // one entry per six contributions of a target
+          for (size_t x0 = u; x0 < w; x0 += 6) {
+            const size_t x1 = std::min(w, x0 + 6);
+            uint32_t c6[6] = {0, 0, 0, 0, 0, 0};
+            for (size_t x = x0; x < x1; x++) c6[x - x0] = items[x].second;
+            tent.push_back(make_int4(items[u].first | (int)((x1 - x0) << 16), (int)(c6[0] | (c6[1] << 16)),
+                                     (int)(c6[2] | (c6[3] << 16)), (int)(c6[4] | (c6[5] << 16))));
+          }
+          u = w;
+        }
+        if (tent.size() > (size_t)INT32_MAX / 2) {
+          set_error("sigma32 tensor-core path: scatter lists too large");
+          return PQ_ERR_ARG;
+        }
+        toff[t + 1] = (int32_t)tent.size();
+      }
+      if (tent.empty()) tent.push_back(make_int4(0, 0, 0, 0));
+      PQ_TRY(upload(h->tc_toff, toff, st));
+      PQ_TRY(upload(h->tc_tinfo, tent, st));
+      h->tc_btab.release();  // the table itself is no longer needed
+      PQ_CUDA_TRY(cudaStreamSynchronize(st));
+    }
     std::vector<float> e((size_t)npair * npair);
     PQ_CUDA_TRY(cudaMemcpyAsync(e.data(), h->d_eab32.ptr, sizeof(float) * e.size(), cudaMemcpyDeviceToHost, st));
     PQ_CUDA_TRY(cudaStreamSynchronize(st));
@@ -609,7 +713,8 @@ static pq_status ab_tc_impl(pq_ci_handle *h, const float *X, float *Y) {
   a.npair = npair;
   a.n_off = n * (n - 1) / 2;
   a.sw = h->tc_sw;
-  a.btab = h->tc_btab.as<uint16_t>();
+  a.t_off = h->tc_toff.as<int32_t>();
+  a.tent = h->tc_tinfo.as<int4>();
   a.wait_cycles = WAIT_CYCLES;
   a.err = err;
 #ifdef PQ_ABTC_PROFILE

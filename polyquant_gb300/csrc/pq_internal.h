@@ -115,6 +115,7 @@ struct pq_ci_handle {
   // FP32 alpha-beta doubles on the tensor cores (ci_sigma32_tc.cu): beta scatter table, scale of the
   // integrals, error word and max |X|
   pq::DevBuf tc_btab, tc_aux;
+  pq::DevBuf tc_toff, tc_tinfo;  // per tile of 32 beta strings: scatter targets and their contributions
   float tc_sw = 1.0f;
   int tc_sms = 0;
   bool tc_ready = false;
