@@ -14,7 +14,8 @@ Printed JSON line (rank 0):
              against the measured HBM copy bandwidth; `fp64` adds the FMA rate against a live DGEMM
   time_to_1uEh : FP64 vs mixed Davidson for the lowest 4 roots (residual 1e-4), each energy's error
              against a 1e-7 FP64 solve
-  psh_like : the electron-positron product space (60 x 40 orbitals, 144,000 determinants)
+  psh_like : the electron-positron product space (60 x 40 orbitals, 144,000 determinants); its heat_bath
+             entry is the selected-string extension (nested thresholds, energies against the full product)
   ao2mo    : AO->MO transform at N = 256 (BF16x3, TF32x3, FP64)
   batched_ci : the batched uneven-CI workload (by default the first 32 of its 256 seeded problems;
              --batch-problems 256 runs all)
@@ -375,6 +376,17 @@ def bench_psh_like(seed=0, cpu_budget=5.0):
     res["davidson_mixed_sigma_calls"] = [i32["sigma_calls_fp64"], i32["sigma_calls_fp32"]]
     res["max_abs_energy_error_mixed"] = float(np.abs(e32 - e64).max())
     ds.close()
+    # extension with no reference counterpart: heat-bath selection over strings on the same space, nested
+    # thresholds, each variational energy against the full product's
+    from polyquant_gb300.heatbath import heat_bath_ci
+
+    prob = dict(n_orb=args[0], n_alpha=args[1], n_beta=args[2], h1=args[3], eri=args[4], **kw)
+    t0 = time.perf_counter()
+    hb = heat_bath_ci(prob, [1e-2, 1e-3, 1e-4, 1e-5], convergence_E=1e-8)
+    res["heat_bath"] = {"note": "extension: selected-string CI (polyquant_gb300/heatbath.py), nested thresholds",
+                        "seconds": time.perf_counter() - t0, "full_product_E0": float(e64[0]),
+                        "steps": [{"eps": r["eps"], "E0": r["energies"][0], "n_dets": r["n_dets"],
+                                   "error_vs_full": r["energies"][0] - float(e64[0])} for r in hb]}
     # CPU baseline: the oracle's gather sigma on a row sample of the same space and vectors
     ref = O.Detset(O.CIProblem(*args, **kw))
     C = np.asfortranarray(X.cpu().numpy())

@@ -81,6 +81,17 @@ typedef struct pq_ci_handle pq_ci_handle;
  * on the device (replaces setup_determinants + precompute_diagonal).
  * stream: a cudaStream_t, or NULL for the default stream. */
 pq_status pq_ci_create(const pq_ci_desc *desc, void *stream, pq_ci_handle **out);
+/* Selected-string space (an extension with no reference counterpart: heat-bath
+ * selected CI over strings, polyquant_gb300/heatbath.py): the determinants are
+ * the full product of caller-chosen string lists, in list order (species 0
+ * alpha outermost).  strings[2 s + spin] holds n_strings[2 s + spin]
+ * occupation masks (bit o = orbital o; at most 64 orbitals; each with the
+ * species' particle count for that spin; no duplicates).  desc supplies the
+ * orbitals, particle counts, integrals and charges; its excitation levels and
+ * collective limit are ignored.  Everything else (sigma, Davidson, explicit H,
+ * elements, properties) works on the handle as on any other. */
+pq_status pq_ci_create_selected(const pq_ci_desc *desc, const uint64_t *const *strings, const int64_t *n_strings,
+                                void *stream, pq_ci_handle **out);
 pq_status pq_ci_destroy(pq_ci_handle *h);
 
 /* rows() == cols() == number of determinants. */

@@ -17,7 +17,7 @@ PQ_AO_PACKED8, PQ_AO_PAIRS = 0, 1
 PQ_XFORM_FP64, PQ_XFORM_BF16X3, PQ_XFORM_TF32X3 = 0, 1, 2
 
 EXPORTS = [
-    "pq_last_error", "pq_version", "pq_ci_create", "pq_ci_destroy", "pq_ci_num_dets", "pq_ci_strings",
+    "pq_last_error", "pq_version", "pq_ci_create", "pq_ci_create_selected", "pq_ci_destroy", "pq_ci_num_dets", "pq_ci_strings",
     "pq_ci_det_unfold", "pq_ci_diag", "pq_ci_sigma", "pq_ci_sigma_host", "pq_ci_sigma_noalloc",
     "pq_ci_sigma_interleaved", "pq_ci_element", "pq_ci_elements", "pq_debug_scratch_bytes",
     "pq_ci_davidson", "pq_ci_ham_build", "pq_ci_ham_release", "pq_ci_ham_csr", "pq_ci_s2", "pq_ci_rdm1",
@@ -91,6 +91,8 @@ def load(path: str = LIB_PATH):
     L.pq_version.restype = ctypes.c_char_p
     L.pq_ci_create.restype = I32
     L.pq_ci_create.argtypes = [ctypes.POINTER(PQDesc), P, ctypes.POINTER(P)]
+    L.pq_ci_create_selected.restype = I32
+    L.pq_ci_create_selected.argtypes = [ctypes.POINTER(PQDesc), P, P, P, ctypes.POINTER(P)]
     L.pq_ci_destroy.restype = I32
     L.pq_ci_destroy.argtypes = [P]
     L.pq_ci_num_dets.restype = I32

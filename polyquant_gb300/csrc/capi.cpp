@@ -1,6 +1,7 @@
 // extern "C" entry points of libpq_gb300 (declared in include/pq_ci.h and
 // include/pq_ints.h).  Argument checking, error reporting and handle lifetime
 // live here; the work is in the .cu translation units.
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -57,6 +58,72 @@ pq_status pq_ci_create(const pq_ci_desc *desc, void *stream, pq_ci_handle **out)
   if (s != PQ_OK) {
     delete h;
     return s;
+  }
+  *out = h;
+  return PQ_OK;
+}
+
+pq_status pq_ci_create_selected(const pq_ci_desc *desc, const uint64_t *const *strings, const int64_t *n_strings,
+                                void *stream, pq_ci_handle **out) {
+  clear_error();
+  if (!desc || !strings || !n_strings || !out || desc->n_species < 1 || desc->n_species > 2) {
+    set_error("pq_ci_create_selected: bad arguments");
+    return PQ_ERR_ARG;
+  }
+  *out = nullptr;
+  // check the lists before anything touches the device
+  for (int s = 0; s < desc->n_species; s++) {
+    const int no = desc->n_orb[s];
+    if (no < 1 || no > 64) {
+      set_error("pq_ci_create_selected: n_orb[%d]=%d outside 1..64", s, no);
+      return PQ_ERR_ARG;
+    }
+    const int ne[2] = {desc->n_alpha[s], desc->n_beta[s]};
+    for (int sp = 0; sp < 2; sp++) {
+      const int64_t n = n_strings[2 * s + sp];
+      const uint64_t *w = strings[2 * s + sp];
+      if (n < 1 || n > INT32_MAX / 2 || !w) {
+        set_error("pq_ci_create_selected: species %d spin %d: %lld strings", s, sp, (long long)n);
+        return PQ_ERR_ARG;
+      }
+      const uint64_t outside = no >= 64 ? 0ULL : ~((1ULL << no) - 1ULL);
+      std::vector<uint64_t> sorted(w, w + n);
+      for (uint64_t m : sorted)
+        if ((m & outside) || __builtin_popcountll(m) != ne[sp]) {
+          set_error("pq_ci_create_selected: species %d spin %d: string %#llx is not %d of %d orbitals", s, sp,
+                    (unsigned long long)m, ne[sp], no);
+          return PQ_ERR_ARG;
+        }
+      std::sort(sorted.begin(), sorted.end());
+      if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end()) {
+        set_error("pq_ci_create_selected: species %d spin %d: a string appears twice", s, sp);
+        return PQ_ERR_ARG;
+      }
+    }
+  }
+  PQ_TRY(check_device());
+  pq_ci_handle *h = new (std::nothrow) pq_ci_handle();
+  if (!h) {
+    set_error("host allocation failed");
+    return PQ_ERR_OOM;
+  }
+  h->desc = *desc;
+  // every string at level 0 and no level limits: the determinant list is the full product, in list order
+  for (int s = 0; s < desc->n_species; s++)
+    for (int t = 0; t < 3; t++) h->desc.ex_level[s][t] = INT32_MAX / 4;
+  h->desc.max_collective = INT32_MAX / 4;
+  h->selected = true;
+  for (int s = 0; s < desc->n_species; s++)
+    for (int sp = 0; sp < 2; sp++) {
+      const int64_t n = n_strings[2 * s + sp];
+      h->str[s][sp].assign(strings[2 * s + sp], strings[2 * s + sp] + n);
+      h->lvl[s][sp].assign(n, 0);
+    }
+  h->stream = (cudaStream_t)stream;
+  pq_status st = ci_build(h);
+  if (st != PQ_OK) {
+    delete h;
+    return st;
   }
   *out = h;
   return PQ_OK;

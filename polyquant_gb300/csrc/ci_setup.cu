@@ -391,7 +391,11 @@ pq_status ci_build(pq_ci_handle *h) {
   // second word is kept only when some species has more than 64 orbitals
   h->n_words = (maxorb >> 6) + 1;
   h->wide = maxorb > 64;
-  for (int s = 0; s < d.n_species; s++) {
+  if (h->selected && h->wide) {
+    set_error("selected string lists hold at most 64 orbitals per species");
+    return PQ_ERR_ARG;
+  }
+  for (int s = 0; s < d.n_species && !h->selected; s++) {
     int ne[2] = {d.n_alpha[s], d.n_beta[s]};
     for (int sp = 0; sp < 2; sp++)
       PQ_TRY(make_strings(d.n_orb[s], ne[sp], d.ex_level[s][sp], h->str[s][sp], h->lvl[s][sp],

@@ -379,7 +379,11 @@ pq_status ci_build2(pq_ci_handle *h) {
   }
   h->n_words = (maxorb >> 6) + 1;
   h->wide = maxorb > 64;
-  for (int s = 0; s < 2; s++) {
+  if (h->selected && h->wide) {
+    set_error("selected string lists hold at most 64 orbitals per species");
+    return PQ_ERR_ARG;
+  }
+  for (int s = 0; s < 2 && !h->selected; s++) {
     int ne[2] = {d.n_alpha[s], d.n_beta[s]};
     for (int sp = 0; sp < 2; sp++)
       PQ_TRY(make_strings(d.n_orb[s], ne[sp], d.ex_level[s][sp], h->str[s][sp], h->lvl[s][sp],

@@ -90,6 +90,7 @@ struct pq_ci_handle {
   int npair[2] = {0, 0};
   int n_words = 1;     // words per string in the reference layout, (max n_orb >> 6) + 1
   bool wide = false;   // some species has more than 64 orbitals: strings keep a second word
+  bool selected = false;  // strings given by the caller (pq_ci_create_selected): full product, no levels
   int n_blocks[2] = {1, 1};  // spin blocks of integrals per species
   // host strings (occupation masks, reference order) and their levels
   std::vector<uint64_t> str[2][2];

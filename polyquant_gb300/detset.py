@@ -82,16 +82,33 @@ class POLYQUANT_DETSET:
     Scalar = float
 
     def __init__(self, n_orb: Sequence[int], n_alpha: Sequence[int], n_beta: Sequence[int], h1, eri: Dict,
-                 excitation_level: Sequence[Sequence[int]], restricted: Sequence[int] = None,
-                 charge: Sequence[float] = None, max_collective_excitation_level: int = INT_MAX, stream=None):
+                 excitation_level: Sequence[Sequence[int]] = None, restricted: Sequence[int] = None,
+                 charge: Sequence[float] = None, max_collective_excitation_level: int = INT_MAX, stream=None,
+                 selected_strings: Sequence[Sequence] = None):
+        """``selected_strings[s][spin]`` (optional): occupation masks (bit o = orbital o) of a selected-string
+        space (``pq_ci_create_selected``, an extension: the determinants are the full product of these lists
+        and ``excitation_level`` is ignored)."""
         L = _lib.load()
         ns = len(n_orb)
+        if excitation_level is None:
+            if selected_strings is None:
+                raise ValueError("excitation_level is required unless selected_strings is given")
+            excitation_level = [[0, 0, 0]] * ns
         d, self._keep = make_desc(n_orb, n_alpha, n_beta, h1, eri, excitation_level, restricted, charge,
                                   max_collective_excitation_level)
         self._desc = d
         self._stream = stream
         h = ctypes.c_void_p()
-        check(L.pq_ci_create(ctypes.byref(d), ctypes.c_void_p(stream or 0), ctypes.byref(h)), "pq_ci_create")
+        if selected_strings is None:
+            check(L.pq_ci_create(ctypes.byref(d), ctypes.c_void_p(stream or 0), ctypes.byref(h)), "pq_ci_create")
+        else:
+            lists = [np.ascontiguousarray(np.asarray(selected_strings[s][sp], dtype=np.uint64))
+                     for s in range(ns) for sp in range(2)]
+            ptrs = (ctypes.c_void_p * len(lists))(*[a.ctypes.data for a in lists])
+            counts = (ctypes.c_int64 * len(lists))(*[len(a) for a in lists])
+            check(L.pq_ci_create_selected(ctypes.byref(d), ptrs, counts, ctypes.c_void_p(stream or 0),
+                                          ctypes.byref(h)), "pq_ci_create_selected")
+            del lists
         self._h = h
         self._keep = []  # integrals were copied to the device
         n = ctypes.c_int64()
