@@ -209,7 +209,7 @@ static pq_status sigma_device(pq_ci_handle *h, const double *C, int64_t ldc, int
   size_t esz = precision == PQ_FP64 ? sizeof(double) : sizeof(float);
   for (int v0 = 0; v0 < nvec; v0 += 4) {
     int nv = nvec - v0 < 4 ? nvec - v0 : 4;
-    int nvp = il_width(h, nv);
+    int nvp = il_width(h, nv, precision);
     size_t bytes = esz * (size_t)nvp * (size_t)(h->n_dets + 1);
     PQ_TRY(h->x_il.ensure(bytes));
     PQ_TRY(h->y_il.ensure(bytes));

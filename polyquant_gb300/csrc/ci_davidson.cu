@@ -494,7 +494,7 @@ pq_status sigma_request_single(pq_ci_handle *h, const SigmaRequest &r) {
   const int64_t n = h->n_dets;
   const unsigned g = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16);
   for (int v0 = 0; v0 < r.cnt; v0 += 4) {
-    const int c = std::min(4, r.cnt - v0), nvp = il_width(h, c);
+    const int c = std::min(4, r.cnt - v0), nvp = il_width(h, c, r.precision);
     const size_t esz = r.precision == PQ_FP64 ? sizeof(double) : sizeof(float);
     PQ_TRY(h->x_il.ensure(esz * nvp * (size_t)(n + 1)));
     PQ_TRY(h->y_il.ensure(esz * nvp * (size_t)(n + 1)));

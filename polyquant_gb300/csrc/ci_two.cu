@@ -81,6 +81,14 @@ template <typename T, int NV> __device__ __forceinline__ void axpy_gather(T (&ac
 #pragma unroll
   for (int v = 0; v < NV; v++) acc[v] = fma(c, __ldg(X + j * NV + v), acc[v]);
 }
+// four FP32 roots: one 16-byte load (the interleaved rows are 16-byte aligned)
+template <> __device__ __forceinline__ void axpy_gather<float, 4>(float (&acc)[4], float c, const float *X, int64_t j) {
+  const float4 x = __ldg(reinterpret_cast<const float4 *>(X) + j);
+  acc[0] = fmaf(c, x.x, acc[0]);
+  acc[1] = fmaf(c, x.y, acc[1]);
+  acc[2] = fmaf(c, x.z, acc[2]);
+  acc[3] = fmaf(c, x.w, acc[3]);
+}
 
 // sum over occupied orbitals k of the string (m, mh) of M[row * ld + tri(k,k)] (row fixed) or
 // M[tri(k,k) * ld + col]

@@ -170,10 +170,11 @@ pq_status ci_ham_spmv(pq_ci_handle *h, const void *X, void *Y, int nvp);
 pq_status ci_unit_columns(pq_ci_handle *h, const std::vector<int64_t> &dets, double *W);
 // ci_element.cu: exact H_IJ of n pairs (host index arrays, host output)
 pq_status ci_elements(pq_ci_handle *h, int64_t n, const int64_t *I, const int64_t *J, double *out);
-// interleave width of a block of nv <= 4 vectors: 1, 2 or 4; two-species spaces also take 3 (their sigma
-// gathers root by root, so a padded fourth root would only add work)
-inline int il_width(const pq_ci_handle *h, int nv) {
-  if (nv == 3 && h->n_species == 2) return 3;
+// interleave width of a block of nv <= 4 vectors: 1, 2 or 4; two-species spaces take 3 in FP64 (their FP64
+// sigma is bound by the FP64 pipe, so a padded fourth root would only add FMAs), while in FP32 four roots
+// load as one 16-byte vector
+inline int il_width(const pq_ci_handle *h, int nv, int precision) {
+  if (nv == 3 && h->n_species == 2 && precision == PQ_FP64) return 3;
   return nv == 1 ? 1 : (nv == 2 ? 2 : 4);
 }
 // ci_sigma32.cu
