@@ -23,6 +23,7 @@
 // their same-species and cross-species Coulomb terms, same-spin doubles,
 // alpha-beta doubles within a species, single x single cross doubles).
 #include <algorithm>
+#include <type_traits>
 
 #include "pq_bits.cuh"
 #include "pq_internal.h"
@@ -129,7 +130,13 @@ __device__ __forceinline__ double flip2(double v, uint32_t neg) {
 template <bool FULL = false, typename T, typename F>
 __device__ __forceinline__ void two_conn_visit(const Args2<T> &p, const int (&t)[4], const uint64_t (&m)[4],
                                                const uint64_t (&mh)[4], F &&f) {
-  for (int s = 0; s < 4; s++) {
+  // FP32: the slot loops are unrolled, so slots are constants and the string-index arrays stay in registers
+  // (34 % faster on the PsH-like space); the FP64 kernel is bound by its FP64 pipe and keeps the compact
+  // loops and its register count
+  constexpr bool UNROLL = std::is_same<T, float>::value;
+  // the connections of one slot s (its singles, their single x single partners in later slots, its
+  // same-spin doubles)
+  auto slot = [&](const int s) {
     const int sp = s >> 1, spin = s & 1, other = s ^ 1;
     const List2<T> &ls = p.l[s];
     const int np = p.npair[sp];
@@ -159,7 +166,7 @@ __device__ __forceinline__ void two_conn_visit(const Args2<T> &p, const int (&t)
         f(j, h);
       }
       // single x single in a later slot r
-      for (int r = s + 1; r < 4; r++) {
+      auto pair_with = [&](const int r) {
         const List2<T> &lr = p.l[r];
         const int64_t q0 = lr.s1_off[t[r]], q1 = lr.s1_off[t[r] + 1];
         for (int64_t g = q0; g < q1; g++) {
@@ -178,6 +185,12 @@ __device__ __forceinline__ void two_conn_visit(const Args2<T> &p, const int (&t)
           c = flip2(c, neg ^ (uint32_t)(info2 & 1));
           f(k, c);
         }
+      };
+      if constexpr (UNROLL) {
+#pragma unroll
+        for (int r = s + 1; r < 4; r++) pair_with(r);
+      } else {
+        for (int r = s + 1; r < 4; r++) pair_with(r);
       }
     }
     // same-spin doubles in slot s
@@ -188,6 +201,12 @@ __device__ __forceinline__ void two_conn_visit(const Args2<T> &p, const int (&t)
       const int64_t j = lookup2<T, FULL>(p, tj);
       if (j >= 0) f(j, __ldg(ls.s2_D + e));
     }
+  };
+  if constexpr (UNROLL) {
+#pragma unroll
+    for (int s = 0; s < 4; s++) slot(s);
+  } else {
+    for (int s = 0; s < 4; s++) slot(s);
   }
 }
 
