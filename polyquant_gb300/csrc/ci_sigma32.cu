@@ -13,7 +13,8 @@
 //   For four vectors of a full-CI space whose doubles fill at least 3 % of a
 //   row, the same-spin doubles of both sides are instead dense GEMMs on the
 //   tcgen05 tensor cores (ci_sigma32_ss.cu) and passes 1-2 keep the diagonal
-//   and the singles.
+//   and the singles, whose opposite-spin Coulomb sums then come from a
+//   precomputed [pair][column string] table.
 //   3. alpha-beta doubles: for blocks of four vectors, up to 16 orbitals and
 //      64 alpha singles per string, a GEMM per alpha string on the tcgen05
 //      tensor cores (ci_sigma32_tc.cu).  Otherwise input-stationary on the CUDA cores: CTA
