@@ -156,8 +156,9 @@ pq_status pq_ci_sigma_interleaved(pq_ci_handle *h, const void *X, void *Y, int32
                                   double diag_shift);
 
 /* Diagnostic, no reference counterpart: device bytes the handle holds as
- * grow-on-demand work memory (the interleaved vectors of pq_ci_sigma and the
- * transposed copies of the FP32 full-CI sigma).  Meant for tests. */
+ * grow-on-demand work memory (the interleaved vectors of pq_ci_sigma, the
+ * host-sigma staging copies, the transposed copies, tensor-core tables and
+ * same-spin GEMM buffers of the FP32 full-CI sigma).  Meant for tests. */
 pq_status pq_debug_scratch_bytes(const pq_ci_handle *h, int64_t *bytes);
 
 /* Block Davidson on the GPU (replaces Spectra::DavidsonSymEigsSolver with the

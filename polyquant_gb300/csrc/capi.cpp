@@ -295,7 +295,7 @@ pq_status pq_debug_scratch_bytes(const pq_ci_handle *h, int64_t *bytes) {
     return PQ_ERR_ARG;
   }
   *bytes = (int64_t)(h->x_il.bytes + h->y_il.bytes + h->x_t.bytes + h->z_t.bytes + h->tc_btab.bytes + h->tc_aux.bytes +
-                     h->host_c.bytes + h->host_s.bytes);
+                     h->tc_toff.bytes + h->tc_tinfo.bytes + h->host_c.bytes + h->host_s.bytes + ci_sigma32_ss_bytes(h));
   return PQ_OK;
 }
 

@@ -566,6 +566,14 @@ const float *ci_sigma32_ss_coulomb(const pq_ci_handle *h, int spin_row) {
 
 pq_status ci_sigma32_ss_prepare(pq_ci_handle *h) { return ss_prepare(h); }
 
+size_t ci_sigma32_ss_bytes(const pq_ci_handle *h) {
+  if (!h->ss) return 0;
+  const SameSpinGemm &g = *h->ss;
+  size_t b = g.op_hi.bytes + g.op_lo.bytes + g.aux.bytes + g.coul[0].bytes + g.coul[1].bytes;
+  for (const SameSpinGemm::Side &s : g.side) b += s.hi.bytes + s.lo.bytes + s.kt_off.bytes + s.kt_list.bytes;
+  return b;
+}
+
 static pq_status ss_prepare(pq_ci_handle *h) {
   if (h->ss) return PQ_OK;
   SameSpinGemm *g = new (std::nothrow) SameSpinGemm();

@@ -188,6 +188,7 @@ bool sigma32_ss_applicable(const pq_ci_handle *h);
 pq_status ci_sigma32_same_spin_tc(pq_ci_handle *h, const float *X, float *Y);
 pq_status ci_sigma32_ss_prepare(pq_ci_handle *h);
 const float *ci_sigma32_ss_coulomb(const pq_ci_handle *h, int spin_row);
+size_t ci_sigma32_ss_bytes(const pq_ci_handle *h);  // device bytes of the same-spin GEMM state (0 before use)
 pq_status ci_to_il(pq_ci_handle *h, const double *C, int64_t ldc, int v0, int nv, int nvp, int precision, void *X);
 pq_status ci_from_il(pq_ci_handle *h, const void *Y, int v0, int nv, int nvp, int precision, double *S, int64_t lds);
 // ci_davidson.cu

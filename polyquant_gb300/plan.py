@@ -21,8 +21,17 @@ reference's choice max(2 * num_subspace_vec, 10 * num_states)
 ``precision=PQ_FP32`` (mixed) on a one-species full-CI space the FP32 sigma
 adds its two transposed vector copies (4 FP32 values per determinant each);
 with ``explicit_nnz`` (an explicit matrix built for sigma) the CSR arrays
-(12 B per stored entry plus 8 B per row) are counted too.  Handle tables, the
+(12 B per stored entry plus 8 B per row) are counted too, and with
+``same_spin`` = (n_orb, n_alpha, n_beta, restricted) the buffers of the FP32
+same-spin tensor-core GEMMs (``fp32_same_spin_bytes``).  Handle tables, the
 diagonal (8 B per determinant) and the caller's own vectors come on top.
+
+``fp32_same_spin_bytes`` is what the FP32 full-CI sigma of a one-species space
+allocates on its first call when its same-spin doubles run as dense GEMMs
+(ci_sigma32_ss.cu, the same applicability test): the FP16 hi/lo copies of the
+dense doubles matrix of each spin list (shared by both spins when the lists
+and integrals coincide), the FP16 hi/lo vector operand, the two Coulomb tables
+of the singles and a bound on the alpha-beta kernel's scatter lists.
 """
 from __future__ import annotations
 
@@ -72,12 +81,38 @@ def count_determinants(n_orb: Sequence[int], n_alpha: Sequence[int], n_beta: Seq
     return sum(c0 * c1 for l0, c0 in enumerate(p0) for l1, c1 in enumerate(p1) if l0 + l1 <= mc)
 
 
+def fp32_same_spin_bytes(n_orb: int, n_alpha: int, n_beta: int, restricted: bool = True) -> int:
+    """Device bytes of the FP32 same-spin GEMM path of a one-species full-CI space (0 when it does not apply:
+    more than 16 orbitals or 64 alpha singles per string for the tensor-core path, fewer than 256 or more than
+    32768 strings of a spin, or doubles filling less than 3 % of a row)."""
+    na_s, nb_s = comb(n_orb, n_alpha), comb(n_orb, n_beta)
+    singles_a = n_alpha * (n_orb - n_alpha)
+    if n_orb > 16 or singles_a > 64 or nb_s >= 32768 or na_s >= 65536:
+        return 0
+    sides = []
+    for n_s, ne in ((na_s, n_alpha), (nb_s, n_beta)):
+        doubles = comb(ne, 2) * comb(n_orb - ne, 2)
+        if n_s < 256 or n_s > 32768 or doubles < 0.03 * n_s:
+            return 0
+        sides.append((n_s, (n_s + 63) // 64 * 64))
+    shared = restricted and n_alpha == n_beta
+    dense = sum(2 * 2 * n_s * ldk for n_s, ldk in (sides[:1] if shared else sides))
+    (na_, ldk_a), (nb_, ldk_b) = sides
+    operand = 2 * 2 * max(4 * nb_ * ldk_a, 4 * na_ * ldk_b)
+    npair = n_orb * (n_orb + 1) // 2
+    coulomb = 4 * npair * (na_ + nb_)
+    scatter_lists = 16 * nb_ * n_beta * (n_orb - n_beta)
+    return dense + operand + coulomb + scatter_lists
+
+
 def davidson_device_bytes(n_dets: int, num_states: int, num_subspace_vec: int = 5, max_subspace: int = 0,
-                          precision: int = 0, full_ci: bool = True, explicit_nnz: int = 0) -> int:
+                          precision: int = 0, full_ci: bool = True, explicit_nnz: int = 0,
+                          same_spin: Sequence = None) -> int:
     """Device bytes of the Davidson work arrays for n_dets determinants (see the module docstring).
     precision: 0 = FP64, 1 = mixed (FP32 sigma with FP64 refinement); full_ci: one-species space with every
     (alpha, beta) pair (the FP32 sigma then keeps transposed copies); explicit_nnz: stored entries of an
-    explicit matrix that sigma multiplies with (0: none)."""
+    explicit matrix that sigma multiplies with (0: none); same_spin: (n_orb, n_alpha, n_beta, restricted) of
+    that space, to count the FP32 same-spin GEMM buffers."""
     k = num_states
     m0 = min(max(num_subspace_vec, k), n_dets)
     m_max = max_subspace if max_subspace > 0 else max(2 * num_subspace_vec, 10 * k)
@@ -86,4 +121,5 @@ def davidson_device_bytes(n_dets: int, num_states: int, num_subspace_vec: int = 
     sigma_work = 2 * 8 * 4 * (n_dets + 1)
     fp32_transposed = 2 * 4 * 4 * (n_dets + 1) if precision == 1 and full_ci else 0
     csr = (12 * explicit_nnz + 8 * (n_dets + 1)) if explicit_nnz > 0 else 0
-    return vectors + sigma_work + fp32_transposed + csr
+    ss = fp32_same_spin_bytes(*same_spin) if (precision == 1 and full_ci and same_spin is not None) else 0
+    return vectors + sigma_work + fp32_transposed + csr + ss

@@ -43,3 +43,22 @@ def test_davidson_bytes():
     assert davidson_device_bytes(n, 4, 20, precision=1) == base + 2 * 16 * (n + 1)
     assert davidson_device_bytes(n, 4, 20, precision=1, full_ci=False) == base
     assert davidson_device_bytes(100, 2, 5, explicit_nnz=1000) == davidson_device_bytes(100, 2, 5) + 12000 + 808
+
+
+def test_fp32_same_spin_bytes_counts_the_gemm_buffers():
+    """The FP32 same-spin GEMM buffers of FCI(16o, 8a8b): one shared dense doubles matrix (12 870 x 12 928,
+    FP16 hi and lo), the vector operand (4 x 12 870 rows of 12 928, FP16 hi and lo), two Coulomb tables and
+    the scatter-list bound; none when the path does not apply."""
+    from polyquant_gb300.plan import davidson_device_bytes, fp32_same_spin_bytes
+
+    n, ldk, npair = 12870, 12928, 136
+    want = 2 * 2 * n * ldk + 2 * 2 * 4 * n * ldk + 4 * npair * 2 * n + 16 * n * 64
+    assert fp32_same_spin_bytes(16, 8, 8) == want
+    # unrestricted integrals: two dense matrices
+    assert fp32_same_spin_bytes(16, 8, 8, restricted=False) == want + 2 * 2 * n * ldk
+    # too few strings, too many orbitals for the tensor-core path
+    assert fp32_same_spin_bytes(10, 5, 4) == 0 and fp32_same_spin_bytes(18, 9, 9) == 0
+    base = davidson_device_bytes(165_636_900, 4, 8, precision=1)
+    assert davidson_device_bytes(165_636_900, 4, 8, precision=1, same_spin=(16, 8, 8, True)) == base + want
+    assert davidson_device_bytes(165_636_900, 4, 8, precision=0, same_spin=(16, 8, 8, True)) == \
+        davidson_device_bytes(165_636_900, 4, 8, precision=0)
