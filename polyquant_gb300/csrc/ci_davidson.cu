@@ -276,7 +276,6 @@ void DavidsonRun::request(const double *src, double *dst, int cnt, int prec, dou
 }
 
 pq_status DavidsonRun::advance() {
-  const double one = 1.0, zero = 0.0;
   pending = false;
   switch (stage) {
     case AFTER_INIT:
