@@ -40,7 +40,20 @@ int use_all(void) {
   st |= pq_ci_ham_release(h);
   st |= pq_ci_s2(h, NULL, n, 1, s2);
   st |= pq_ci_rdm1(h, NULL, 0, 0, NULL);
+  {
+    double v = 0.0;
+    int64_t I = 0, J = 0, bytes = 0;
+    st |= pq_ci_element(h, 0, 0, &v);
+    st |= pq_ci_elements(h, 1, &I, &J, &v);
+    st |= pq_debug_scratch_bytes(h, &bytes);
+  }
   st |= pq_ci_destroy(h);
+  {
+    const uint64_t hf = 3;
+    const uint64_t *lists[2] = {&hf, &hf};
+    const int64_t counts[2] = {1, 1};
+    st |= pq_ci_create_selected(&d, lists, counts, NULL, &h);
+  }
   st |= pq_ci_batch_create(&d, 1, NULL, &b);
   st |= pq_ci_batch_num_dets(b, 0, &n);
   st |= pq_ci_batch_sigma(b, NULL, NULL, 1, NULL, NULL, PQ_FP64);
@@ -49,6 +62,7 @@ int use_all(void) {
   st |= pq_ci_batch_destroy(b);
   st |= pq_ao2mo(NULL, PQ_AO_PACKED8, 1, 1, NULL, 1, 1, NULL, 1, 1, PQ_XFORM_BF16X3, NULL, NULL);
   st |= pq_mo1(NULL, 1, NULL, 1, 1, NULL, NULL);
+  st |= pq_ao2mo_release_workspace();
   st |= pq_debug_set_wait_budget(0);
   return (int)st;
 }
