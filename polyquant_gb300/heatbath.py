@@ -28,7 +28,7 @@ import numpy as np
 
 from .detset import POLYQUANT_DETSET
 
-__all__ = ["heat_bath_ci", "string_excitations", "excitation_bounds"]
+__all__ = ["heat_bath_ci", "gpu_solver", "string_excitations", "excitation_bounds"]
 
 
 def _idx2(i: int, j: int) -> int:
@@ -94,11 +94,36 @@ def _single_element(m: int, h: int, p: int, n: int, h1: np.ndarray, E: np.ndarra
     return v
 
 
+def gpu_solver(problem: dict, num_states: int = 1, convergence_E: float = 1e-9, num_subspace_vec: int = 8):
+    """The default solver of ``heat_bath_ci``: the selected-string space on the GPU (``pq_ci_create_selected``)
+    and its Davidson solve.  Returns (energies, ground-state vector, det_unfold)."""
+    n_orb, na, nb = list(problem["n_orb"]), list(problem["n_alpha"]), list(problem["n_beta"])
+
+    def solve(strings):
+        ds = POLYQUANT_DETSET(n_orb, na, nb, problem["h1"], problem["eri"], restricted=problem.get("restricted"),
+                              charge=problem.get("charge"), selected_strings=strings)
+        try:
+            k = min(num_states, ds.N_dets)
+            if ds.N_dets == 1:
+                return ds.diagonal().cpu().numpy()[:1], np.ones(1), ds.det_unfold()
+            e, vecs, info = ds.davidson(num_states=k, num_subspace_vec=min(max(num_subspace_vec, 2 * k), ds.N_dets),
+                                        convergence_E=convergence_E, return_vectors=True)
+            return np.asarray(e), vecs[:, 0].cpu().numpy(), ds.det_unfold()
+        finally:
+            ds.close()
+
+    return solve
+
+
 def heat_bath_ci(problem: dict, eps: Sequence[float], num_states: int = 1, max_rounds: int = 20,
-                 convergence_E: float = 1e-9, num_subspace_vec: int = 8, e_const: float = 0.0) -> List[dict]:
+                 convergence_E: float = 1e-9, num_subspace_vec: int = 8, e_const: float = 0.0,
+                 solver=None) -> List[dict]:
     """Selected-string CI for a sequence of decreasing thresholds ``eps``.
 
     ``problem``: the POLYQUANT_DETSET arguments (n_orb, n_alpha, n_beta, h1, eri, restricted, charge).
+    ``solver(strings) -> (energies, ground-state vector, det_unfold)`` solves one selected space (default:
+    ``gpu_solver``); the vector and the unfold table are in the space's determinant order (full product of
+    the lists, species 0 alpha outermost).
     Returns one record per threshold: eps, energies (lowest ``num_states``, plus ``e_const``), the number of
     strings of every species and spin, the number of determinants, the selection rounds used and the
     selected strings (``strings[s][spin]``, in determinant order)."""
@@ -106,7 +131,6 @@ def heat_bath_ci(problem: dict, eps: Sequence[float], num_states: int = 1, max_r
     na, nb = list(problem["n_alpha"]), list(problem["n_beta"])
     ns = len(n_orb)
     restricted = list(problem.get("restricted") or [1] * ns)
-    charge = problem.get("charge")
     h1, eri = problem["h1"], problem["eri"]
     if max(n_orb) > 64:
         raise ValueError("heat_bath_ci: selected string lists hold at most 64 orbitals per species")
@@ -116,24 +140,14 @@ def heat_bath_ci(problem: dict, eps: Sequence[float], num_states: int = 1, max_r
     # start: the Hartree-Fock string of every list
     strings = [[[(1 << ne[s][sp]) - 1] for sp in range(2)] for s in range(ns)]
     members = [[set(strings[s][sp]) for sp in range(2)] for s in range(ns)]
+    if solver is None:
+        solver = gpu_solver(problem, num_states, convergence_E, num_subspace_vec)
     out = []
     for e in sorted(eps, reverse=True):
         rounds = 0
         while True:
             rounds += 1
-            ds = POLYQUANT_DETSET(n_orb, na, nb, h1, eri, restricted=restricted, charge=charge,
-                                  selected_strings=strings)
-            k = min(num_states, ds.N_dets)
-            if ds.N_dets == 1:
-                energies = ds.diagonal().cpu().numpy()[:1]
-                c = np.ones(1)
-            else:
-                energies, vecs, info = ds.davidson(num_states=k, num_subspace_vec=min(max(num_subspace_vec, 2 * k),
-                                                                                      ds.N_dets),
-                                                   convergence_E=convergence_E, return_vectors=True)
-                c = vecs[:, 0].cpu().numpy()
-            unfold = ds.det_unfold()
-            ds.close()
+            energies, c, unfold = solver(strings)
             if rounds > max_rounds:
                 break
             added = 0

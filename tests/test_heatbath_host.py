@@ -34,3 +34,46 @@ def test_excitation_bounds_cover_every_partner_block():
     want_p = np.maximum(np.abs(pp).max(axis=1), np.abs(ep.T).max(axis=1))
     assert np.allclose(U[1][0], want_p)
     assert np.array_equal(E[0][0], ee) and np.array_equal(E[1][1], pp)
+
+
+def _oracle_solver(p):
+    """A selected space solved on the host: the oracle's dense H (the reference's Slater-Condon rules)
+    restricted to the selected determinants, in the library's order (full product of the lists, species 0
+    alpha outermost)."""
+    import oracle as O
+
+    ref = O.Detset(p)
+    H = ref.dense_ham()
+    ns = len(p.n_orb)
+    pos = [[{int(m): i for i, m in enumerate(ref.strings(s, sp)[:, -1])} for sp in range(2)] for s in range(ns)]
+    fidx = {tuple(t): i for i, t in enumerate(ref.unfold())}
+
+    def solve(strings):
+        lists = [strings[s][sp] for s in range(ns) for sp in range(2)]
+        unfold = np.array(list(itertools.product(*[range(len(l)) for l in lists])), dtype=np.int32)
+        idx = [fidx[tuple(pos[k // 2][k % 2][lists[k][t[k]]] for k in range(2 * ns))] for t in unfold]
+        w, v = np.linalg.eigh(H[np.ix_(idx, idx)])
+        return w[:1], v[:, 0], unfold
+
+    return solve, np.linalg.eigvalsh(H)[0], ref.n_dets
+
+
+def test_nested_selection_is_monotone_and_reaches_the_full_space():
+    """The driver's selection on the host (oracle solver): energies never rise along decreasing thresholds,
+    the loosest threshold keeps a proper subspace, eps = 0 selects every string and gives the full-space
+    ground state."""
+    from cases import batch_dict, synthetic_fci
+    from polyquant_gb300.heatbath import heat_bath_ci
+
+    for p in (synthetic_fci(7, 2, 2, seed=3), synthetic_ep(6, 1, 1, 5, 1, 0, seed=2)):
+        d = batch_dict(p)
+        prob = {k: d[k] for k in ("n_orb", "n_alpha", "n_beta", "h1", "eri", "restricted", "charge")}
+        solve, e_full, n_full = _oracle_solver(p)
+        recs = heat_bath_ci(prob, [0.1, 1e-2, 1e-3, 0.0], solver=solve)
+        es = [r["energies"][0] for r in recs]
+        assert all(b <= a + 1e-12 for a, b in zip(es, es[1:])), es
+        assert recs[0]["n_dets"] < n_full and recs[-1]["n_dets"] == n_full
+        assert abs(es[-1] - e_full) < 1e-10
+        sizes = [r["n_strings"] for r in recs]
+        for a, b in zip(sizes, sizes[1:]):
+            assert all(b[s][sp] >= a[s][sp] for s in range(len(a)) for sp in range(2))
