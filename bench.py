@@ -668,7 +668,10 @@ def main():
                                        "unit": "GB/s", "frac": bytes32 / (ms32 * 1e-3) / 1e9 / hbm,
                                        "algorithmic_bytes_per_launch": bytes32,
                                        "fp32_fma_per_launch": fmas,
-                                       "fp32_tflops": 2 * fmas / (ms32 * 1e-3) / 1e12}},
+                                       "fp32_tflops": 2 * fmas / (ms32 * 1e-3) / 1e12,
+                                       "note": "the alpha-beta and same-spin doubles run on the tcgen05 tensor "
+                                               "cores (FP16 hi/lo split, FP32 accumulation) where the space "
+                                               "allows; per-kernel ncu figures in profiles/"}},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                              "frac": achieved / hbm, "traffic": FP64_SIGMA_DRAM_BYTES_PER_DET * n,
                              "traffic_note": "ncu dram__bytes_read+write of one FP64 sigma launch on FCI(14o, 7a7b) "
